@@ -1,0 +1,82 @@
+"""Builds the in-tree CUDA library draw_gb300/_lib/libdrawgpu.so for sm_103a.
+
+Floating-point flags are part of the contract with the reference's Rust
+semantics: -fmad=false (no FMA contraction on the device), IEEE division and
+square root, no flush-to-zero, and -ffp-contract=off for the host code (GCC
+contracts by default on aarch64). The kernels also use explicit __f*_rn
+intrinsics on every exact path.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(LIBDIR, "libdrawgpu.so")
+SOURCES = ["dg_kernels.cu", "dg_api.cu"]
+HEADERS = ["dg_internal.cuh"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = [
+    "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "--expt-relaxed-constexpr",
+]
+
+
+def nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found: the draw_gb300 CUDA library cannot be built")
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS]
+    deps.append(os.path.join(HERE, "..", "include", "draw_gpu.h"))
+    deps.append(os.path.abspath(__file__))
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build(force: bool = False, verbose: bool = False, extra: list | None = None) -> str:
+    if not force and not _stale():
+        return LIB
+    os.makedirs(LIBDIR, exist_ok=True)
+    tag = f"{os.getpid()}"
+    objs = []
+    cmds = []
+    for s in SOURCES:
+        obj = os.path.join(LIBDIR, s.replace(".cu", f".{tag}.o"))
+        objs.append(obj)
+        cmds.append([nvcc(), *ARCH, *NVCC_FLAGS, *(extra or []), "-c", os.path.join(CSRC, s), "-o", obj])
+    with cf.ThreadPoolExecutor(len(cmds)) as ex:
+        res = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), cmds))
+    for c, r in zip(cmds, res):
+        if verbose or r.returncode:
+            sys.stderr.write(" ".join(c) + "\n" + r.stdout + r.stderr)
+        if r.returncode:
+            raise RuntimeError(f"nvcc failed on {c[-3]}")
+    tmp = LIB + f".{tag}.tmp"
+    link = [nvcc(), *ARCH, "-shared", *objs, "-o", tmp]
+    r = subprocess.run(link, capture_output=True, text=True)
+    if r.returncode:
+        sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)
+        raise RuntimeError("nvcc link failed")
+    os.replace(tmp, LIB)
+    for o in objs:
+        try:
+            os.remove(o)
+        except OSError:
+            pass
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None))

@@ -1,0 +1,1057 @@
+// dg_api.cu -- host side of the GB300 rasterizer: the C ABI declared in
+// include/draw_gpu.h, resource management in HBM, the per-frame host setup of
+// Scene::render (camera basis, transformation matrix, view planes) and the
+// launch sequence of one render job.
+//
+// Host floating point follows the reference's Rust semantics: this file is
+// compiled with -ffp-contract=off, so every expression below rounds each
+// operation to f32 in source order.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "dg_internal.cuh"
+
+namespace {
+
+// ------------------------------------------------------------ host vectors
+struct HV3 {
+    float x, y, z;
+};
+inline HV3 h3(float x, float y, float z) { return HV3{x, y, z}; }
+inline HV3 hadd(HV3 a, HV3 b) { return h3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline HV3 hsub(HV3 a, HV3 b) { return h3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline HV3 hmul(HV3 a, float s) { return h3(a.x * s, a.y * s, a.z * s); }
+inline HV3 hdiv(HV3 a, float s) { return h3(a.x / s, a.y / s, a.z / s); }
+inline float hdot(HV3 a, HV3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }           // linalg.rs:182-184
+inline float hnorm(HV3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }      // linalg.rs:167-171
+inline HV3 hnormalized(HV3 a) { return hdiv(a, hnorm(a)); }                               // linalg.rs:173-175
+inline HV3 hcross(HV3 a, HV3 b) {                                                          // linalg.rs:186-200
+    return h3((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x));
+}
+
+struct HM4 {
+    float m[4][4];
+};
+HM4 hm_zero() {
+    HM4 r;
+    std::memset(&r, 0, sizeof(r));
+    return r;
+}
+HM4 hm_mul(const HM4& a, const HM4& b) {  // linalg.rs:328-344, accumulator starts at 0.0
+    HM4 c = hm_zero();
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            float acc = 0.0f;
+            for (int k = 0; k < 4; k++) acc = acc + a.m[i][k] * b.m[k][j];
+            c.m[i][j] = acc;
+        }
+    return c;
+}
+void hm_vec(const HM4& a, const float v[4], float out[4]) {  // linalg.rs:346-360
+    for (int i = 0; i < 4; i++) {
+        float acc = 0.0f;
+        for (int j = 0; j < 4; j++) acc = acc + a.m[i][j] * v[j];
+        out[i] = acc;
+    }
+}
+
+const float kRadsPerDeg = 3.14159265358979323846f / 180.0f;  // f32::to_radians
+
+struct Camera {  // scene/mod.rs:282-294
+    HV3 position, direction, up;
+    float top, bottom, right, left;
+    float near_, far_;
+    HV3 u, v, w;
+};
+
+dg_status camera_init(Camera& c, HV3 pos, HV3 dir, float ratio, float near_, float far_, float fov_x) {
+    // Camera::new, scene/mod.rs:297-357
+    float rad = fov_x * kRadsPerDeg;
+    float right = std::fabs(near_) * std::tan(rad / 2.0f);
+    float left = -right;
+    float top = (1.0f / ratio) * right;
+    float bottom = -top;
+    if (!(fov_x < 180.0f) || !(near_ < 0.0f) || !(near_ > far_) || !(right > left) || !(top > bottom))
+        return DG_E_CAMERA;
+    c.position = pos;
+    c.direction = hnormalized(dir);
+    c.up = h3(0.0f, 1.0f, 0.0f);
+    c.top = top;
+    c.bottom = bottom;
+    c.right = right;
+    c.left = left;
+    c.near_ = near_;
+    c.far_ = far_;
+    c.u = c.v = c.w = h3(0.0f, 0.0f, 0.0f);
+    return DG_OK;
+}
+
+void camera_update_basis(Camera& c) {  // scene/mod.rs:438-451
+    HV3 g = c.direction;
+    HV3 w = hmul(hdiv(g, hnorm(g)), -1.0f);
+    HV3 txw = hcross(c.up, w);
+    HV3 u = hdiv(txw, hnorm(txw));
+    HV3 v = hcross(w, u);
+    c.u = hnormalized(u);
+    c.v = hnormalized(v);
+    c.w = hnormalized(w);
+}
+
+dg_status camera_basis(const Camera& c, HM4& b) {  // scene/mod.rs:415-428
+    if (!(hnorm(c.u) > 0.0f && hnorm(c.v) > 0.0f && hnorm(c.w) > 0.0f)) return DG_E_CAMERA;
+    b = hm_zero();
+    const HV3 cols[3] = {c.u, c.v, c.w};
+    for (int j = 0; j < 3; j++) {
+        b.m[0][j] = cols[j].x;
+        b.m[1][j] = cols[j].y;
+        b.m[2][j] = cols[j].z;
+    }
+    b.m[3][3] = 1.0f;
+    return DG_OK;
+}
+
+struct Scene {  // scene/mod.rs:749-757
+    uint64_t width, height;
+    Camera cam;
+    std::vector<int32_t> objects;
+    std::vector<HV3> lights;
+    int32_t exponent;
+};
+
+// gen_transformation_matrix (scene/mod.rs:817-899) and gen_view_planes (:481-593).
+dg_status frame_setup(Scene& s, float M[4][4], float planes[6][4]) {
+    Camera& c = s.cam;
+    const float nx = (float)s.width, ny = (float)s.height;
+    const float n = c.near_, f = c.far_, r = c.right, l = c.left, t = c.top, b = c.bottom;
+    // Camera::gen_matrix, :453-479
+    HM4 tr = hm_zero();
+    tr.m[0][0] = tr.m[1][1] = tr.m[2][2] = tr.m[3][3] = 1.0f;
+    tr.m[0][3] = -c.position.x;
+    tr.m[1][3] = -c.position.y;
+    tr.m[2][3] = -c.position.z;
+    camera_update_basis(c);
+    HM4 basis;
+    dg_status e = camera_basis(c, basis);
+    if (e) return e;
+    HM4 bt = basis;
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) bt.m[i][j] = basis.m[j][i];
+    HM4 view = hm_mul(bt, tr);
+    HM4 persp = hm_zero();
+    persp.m[0][0] = n;
+    persp.m[1][1] = n;
+    persp.m[2][2] = n + f;
+    persp.m[2][3] = -(n * f);
+    persp.m[3][2] = 1.0f;
+    HM4 orth = hm_zero();
+    orth.m[0][0] = 2.0f / (r - l);
+    orth.m[0][3] = -(r + l) / (r - l);
+    orth.m[1][1] = 2.0f / (t - b);
+    orth.m[1][3] = -(t + b) / (t - b);
+    orth.m[2][2] = 2.0f / (n - f);
+    orth.m[2][3] = -(n + f) / (n - f);
+    orth.m[3][3] = 1.0f;
+    HM4 vp = hm_zero();
+    vp.m[0][0] = nx / 2.0f;
+    vp.m[0][3] = (nx - 1.0f) / 2.0f;
+    vp.m[1][1] = ny / 2.0f;
+    vp.m[1][3] = (ny - 1.0f) / 2.0f;
+    vp.m[2][2] = 1.0f;
+    vp.m[3][3] = 1.0f;
+    HM4 full = hm_mul(hm_mul(hm_mul(vp, orth), persp), view);
+    std::memcpy(M, full.m, sizeof(full.m));
+
+    // view planes
+    camera_update_basis(c);
+    e = camera_basis(c, basis);
+    if (e) return e;
+    auto world = [&](float x, float y, float z) {
+        float in[4] = {x, y, z, 1.0f}, out[4];
+        hm_vec(basis, in, out);
+        return hadd(h3(out[0] / out[3], out[1] / out[3], out[2] / out[3]), c.position);
+    };
+    HV3 urn = world(r, t, n), uln = world(l, t, n), lrn = world(r, b, n), lln = world(l, b, n);
+    float xc = (l + r) / 2.0f, yc = (b + t) / 2.0f;
+    HV3 ucf = world(xc, (f * t) / n, f), lcf = world(xc, (f * b) / n, f);
+    HV3 rcf = world((f * r) / n, yc, f), lfc = world((f * l) / n, yc, f);
+    HV3 vis = hdiv(hadd(urn, lcf), 2.0f);
+    const HV3 pts[6][3] = {{urn, lrn, lln}, {lfc, rcf, ucf}, {rcf, urn, lrn},
+                           {lfc, lln, uln}, {ucf, uln, urn}, {lcf, lln, lrn}};
+    for (int p = 0; p < 6; p++) {  // ViewPlane::new, :603-632
+        HV3 pv = hsub(pts[p][1], pts[p][0]);
+        HV3 qv = hsub(pts[p][2], pts[p][1]);
+        HV3 nn = hcross(pv, qv);
+        float k = -hdot(nn, pts[p][0]);
+        float tv = hdot(nn, vis) + k;
+        if (tv < 0.0f) {
+            nn = hcross(qv, pv);
+            k = -hdot(nn, pts[p][0]);
+            tv = hdot(nn, vis) + k;
+            if (!(tv > 0.0f)) return DG_E_CAMERA;
+        }
+        planes[p][0] = nn.x;
+        planes[p][1] = nn.y;
+        planes[p][2] = nn.z;
+        planes[p][3] = k;
+    }
+    return DG_OK;
+}
+
+// ------------------------------------------------------------- resources
+struct TexMap {
+    uint32_t* d_words = nullptr;
+    uint64_t len = 0;
+    uint32_t w = 0, h = 0, comps = 0;
+};
+
+struct Object {
+    bool alive = false;
+    float4* d_pos = nullptr;
+    float4* d_nrm = nullptr;
+    float2* d_uv = nullptr;
+    uint4* d_tri_pos = nullptr;
+    uint4* d_tri_uv = nullptr;
+    uint4* d_tri_nrm = nullptr;
+    DgMatDev* d_mats = nullptr;
+    uint32_t nv = 0, nn = 0, nuv = 0, ntri_opaque = 0, nmats = 0;
+    std::vector<float> h_pos;                        // for the transparent pass sort
+    std::vector<std::vector<uint32_t>> transparent;  // 9 indices per triangle, current order
+    std::vector<int32_t> transparent_mat;
+};
+
+struct Canvas {
+    bool alive = false;
+    uint64_t w = 0, h = 0;
+    uint32_t* d_colour = nullptr;
+    float* d_depth = nullptr;
+    uint64_t* d_vis = nullptr;
+    bool depth_init = false;
+    float depth_max = 0.0f;
+    float off_x = 0.0f, off_y = 0.0f;
+};
+
+}  // namespace
+
+struct dg_ctx {
+    int device = 0;
+    int nsm = 152;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::vector<TexMap> tex;  // [0] = 1x1 white default map
+    DgTexDev* d_tex = nullptr;
+    size_t d_tex_cap = 0;
+    bool tex_dirty = true;
+    std::vector<Object> objects;
+    std::vector<Scene> scenes;
+    std::vector<Canvas> canvases;
+    // render scratch
+    float4* d_vrec = nullptr;
+    size_t vrec_cap = 0;
+    float4* d_vshade = nullptr;
+    size_t vshade_cap = 0;
+    DgLargeRec* d_large = nullptr;
+    uint32_t* d_large_base = nullptr;
+    size_t large_cap = 0;
+    unsigned long long* d_counters = nullptr;  // [0] large counter, [1] covered px, [2] overflow
+    uint32_t* d_err = nullptr;
+    // job descriptors: pinned staging ring + device copies
+    static const int kSlots = 4;
+    void* h_stage[kSlots] = {};
+    void* d_stage[kSlots] = {};
+    size_t stage_cap[kSlots] = {};
+    cudaEvent_t stage_ev[kSlots] = {};
+    int slot = 0;
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[5] = {};
+    bool ev_valid = false;
+    uint64_t last_vtx = 0, last_tri = 0;
+};
+
+namespace {
+
+dg_status cuda_ok(cudaError_t e) { return e == cudaSuccess ? DG_OK : DG_E_CUDA; }
+#define DG_CUDA(x)                                      \
+    do {                                                \
+        cudaError_t _e = (x);                           \
+        if (_e != cudaSuccess) {                        \
+            return _e == cudaErrorMemoryAllocation ? DG_E_OOM : DG_E_CUDA; \
+        }                                               \
+    } while (0)
+
+template <class T>
+dg_status dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? DG_E_OOM : DG_E_CUDA;
+    }
+    return DG_OK;
+}
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+dg_status set_device(dg_ctx* c) {
+    if (c->device < 0) return DG_E_CUDA;  // host-only context: no device work
+    return cuda_ok(cudaSetDevice(c->device));
+}
+
+dg_status tex_upload(dg_ctx* c, const uint8_t* img, uint64_t len, uint32_t w, uint32_t h, uint32_t comps,
+                     TexMap& out) {
+    uint64_t nwords = (len + 3) / 4 + 1;
+    std::vector<uint32_t> words(nwords, 0u);
+    if (len) std::memcpy(words.data(), img, len);
+    dg_status e = dalloc(&out.d_words, nwords);
+    if (e) return e;
+    DG_CUDA(cudaMemcpy(out.d_words, words.data(), nwords * 4, cudaMemcpyHostToDevice));
+    out.len = len;
+    out.w = w;
+    out.h = h;
+    out.comps = comps;
+    return DG_OK;
+}
+
+dg_status sync_tex_table(dg_ctx* c) {
+    if (!c->tex_dirty) return DG_OK;
+    std::vector<DgTexDev> t(c->tex.size());
+    for (size_t i = 0; i < c->tex.size(); i++) {
+        t[i].words = c->tex[i].d_words;
+        t[i].len = c->tex[i].len;
+        t[i].width = c->tex[i].w;
+        t[i].height = c->tex[i].h;
+        t[i].comps = c->tex[i].comps;
+        t[i].fw = (float)c->tex[i].w;
+        t[i].fh = (float)c->tex[i].h;
+    }
+    if (c->d_tex_cap < t.size()) {
+        DG_CUDA(cudaStreamSynchronize(c->stream));
+        dfree(c->d_tex);
+        size_t cap = std::max<size_t>(16, t.size() * 2);
+        dg_status e = dalloc(&c->d_tex, cap);
+        if (e) return e;
+        c->d_tex_cap = cap;
+    } else {
+        DG_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    DG_CUDA(cudaMemcpy(c->d_tex, t.data(), t.size() * sizeof(DgTexDev), cudaMemcpyHostToDevice));
+    c->tex_dirty = false;
+    return DG_OK;
+}
+
+template <class T>
+dg_status grow(dg_ctx* c, T** p, size_t* cap, size_t need) {
+    if (*cap >= need && *p) return DG_OK;
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    dfree(*p);
+    size_t n = std::max(need, (size_t)(*cap * 3 / 2));
+    dg_status e = dalloc(p, n);
+    if (e) {
+        *cap = 0;
+        return e;
+    }
+    *cap = n;
+    return DG_OK;
+}
+
+Scene* get_scene(dg_ctx* c, int32_t id) {
+    if (!c || id < 0 || (size_t)id >= c->scenes.size()) return nullptr;
+    return &c->scenes[id];
+}
+Canvas* get_canvas(dg_ctx* c, int32_t id) {
+    if (!c || id < 0 || (size_t)id >= c->canvases.size() || !c->canvases[id].alive) return nullptr;
+    return &c->canvases[id];
+}
+Object* get_object(dg_ctx* c, int32_t id) {
+    if (!c || id < 0 || (size_t)id >= c->objects.size() || !c->objects[id].alive) return nullptr;
+    return &c->objects[id];
+}
+
+dg_status take_errors(dg_ctx* c) {
+    uint32_t err = 0;
+    DG_CUDA(cudaMemcpy(&err, c->d_err, 4, cudaMemcpyDeviceToHost));
+    if (!err) return DG_OK;
+    uint32_t zero = 0;
+    DG_CUDA(cudaMemcpy(c->d_err, &zero, 4, cudaMemcpyHostToDevice));
+    for (int b = 1; b < 32; b++)
+        if (err & (1u << b)) return (dg_status)b;
+    return DG_E_CUDA;
+}
+
+// Builds and launches one render job over n (scene, canvas) frames.
+dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n) {
+    if (n == 0) return DG_OK;
+    dg_status e = set_device(c);
+    if (e) return e;
+    std::vector<DgFrameDev> frames(n);
+    std::vector<DgSegDev> segs;
+    uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0;
+    uint32_t stride = 1;
+    for (uint32_t i = 0; i < n; i++) {
+        Scene* s = get_scene(c, scenes[i]);
+        Canvas* cv = get_canvas(c, canvases[i]);
+        if (!s || !cv) return DG_E_INVALID;
+        if (!cv->depth_init) return DG_E_DEPTH_UNINIT;
+        for (int32_t oid : s->objects)
+            if (!c->objects[oid].transparent.empty()) return DG_E_LIMIT;
+        DgFrameDev& f = frames[i];
+        std::memset(&f, 0, sizeof(f));
+        e = frame_setup(*s, f.M, f.plane);
+        if (e) return e;
+        f.cam[0] = s->cam.position.x;
+        f.cam[1] = s->cam.position.y;
+        f.cam[2] = s->cam.position.z;
+        f.clear_depth = cv->depth_max;
+        f.nlights = (uint32_t)s->lights.size();
+        for (size_t l = 0; l < s->lights.size(); l++) {
+            f.light[l][0] = s->lights[l].x;
+            f.light[l][1] = s->lights[l].y;
+            f.light[l][2] = s->lights[l].z;
+        }
+        stride = std::max(stride, f.nlights);
+        f.exponent = s->exponent;
+        f.off_x = cv->off_x;
+        f.off_y = cv->off_y;
+        f.width = (uint32_t)cv->w;
+        f.height = (uint32_t)cv->h;
+        f.vis = cv->d_vis;
+        f.colour = cv->d_colour;
+        f.depth = cv->d_depth;
+        f.seg_begin = (uint32_t)segs.size();
+        f.tile_begin = (uint32_t)total_tiles;
+        f.tiles_x = (uint32_t)((cv->w + DG_TILE_W - 1) / DG_TILE_W);
+        total_tiles += (uint64_t)f.tiles_x * ((cv->h + DG_TILE_H - 1) / DG_TILE_H);
+        uint64_t seq = 0;
+        for (int32_t oid : s->objects) {
+            Object& o = c->objects[oid];
+            DgSegDev sg;
+            std::memset(&sg, 0, sizeof(sg));
+            sg.frame = i;
+            sg.tri_begin = (uint32_t)total_tri;
+            sg.vtx_begin = (uint32_t)total_vtx;
+            sg.seq_base = (uint32_t)seq;
+            sg.ntri = o.ntri_opaque;
+            sg.nv = o.nv;
+            sg.nmats = o.nmats;
+            sg.pos = o.d_pos;
+            sg.nrm = o.d_nrm;
+            sg.uv = o.d_uv;
+            sg.tri_pos = o.d_tri_pos;
+            sg.tri_uv = o.d_tri_uv;
+            sg.tri_nrm = o.d_tri_nrm;
+            sg.mats = o.d_mats;
+            segs.push_back(sg);
+            total_tri += o.ntri_opaque;
+            total_vtx += o.nv;
+            seq += o.ntri_opaque;
+        }
+        if (seq >= (1ull << 30)) return DG_E_LIMIT;
+        f.seg_count = (uint32_t)(segs.size() - f.seg_begin);
+    }
+    if (total_tri >= 0xFFFFFFFFull || total_vtx >= 0xFFFFFFFFull || total_tiles >= 0x7FFFFFFFull) return DG_E_LIMIT;
+    if (segs.empty()) {  // keep a valid segment table
+        DgSegDev sg;
+        std::memset(&sg, 0, sizeof(sg));
+        segs.push_back(sg);
+    }
+    e = sync_tex_table(c);
+    if (e) return e;
+    e = grow(c, &c->d_vrec, &c->vrec_cap, std::max<uint64_t>(total_vtx, 1));
+    if (e) return e;
+    e = grow(c, &c->d_vshade, &c->vshade_cap, std::max<uint64_t>(total_vtx * stride * 2, 1));
+    if (e) return e;
+    size_t want_large = std::max<size_t>(1u << 16, (size_t)(total_tri / 4));
+    if (c->large_cap < want_large) {
+        DG_CUDA(cudaStreamSynchronize(c->stream));
+        dfree(c->d_large);
+        dfree(c->d_large_base);
+        c->large_cap = 0;
+        e = dalloc(&c->d_large, want_large);
+        if (e) return e;
+        e = dalloc(&c->d_large_base, want_large);
+        if (e) return e;
+        c->large_cap = want_large;
+    }
+
+    // job descriptor upload through a pinned staging slot
+    size_t fbytes = frames.size() * sizeof(DgFrameDev), sbytes = segs.size() * sizeof(DgSegDev);
+    size_t need = fbytes + sbytes;
+    int slot = c->slot;
+    c->slot = (c->slot + 1) % dg_ctx::kSlots;
+    DG_CUDA(cudaEventSynchronize(c->stage_ev[slot]));
+    if (c->stage_cap[slot] < need) {
+        if (c->h_stage[slot]) cudaFreeHost(c->h_stage[slot]);
+        dfree(c->d_stage[slot]);
+        c->h_stage[slot] = nullptr;
+        c->stage_cap[slot] = 0;
+        size_t cap = std::max<size_t>(need * 2, 64 * 1024);
+        DG_CUDA(cudaMallocHost(&c->h_stage[slot], cap));
+        e = dalloc((uint8_t**)&c->d_stage[slot], cap);
+        if (e) return e;
+        c->stage_cap[slot] = cap;
+    }
+    std::memcpy(c->h_stage[slot], frames.data(), fbytes);
+    std::memcpy((uint8_t*)c->h_stage[slot] + fbytes, segs.data(), sbytes);
+    DG_CUDA(cudaMemcpyAsync(c->d_stage[slot], c->h_stage[slot], need, cudaMemcpyHostToDevice, c->stream));
+    DG_CUDA(cudaEventRecord(c->stage_ev[slot], c->stream));
+
+    DgJobDev job;
+    std::memset(&job, 0, sizeof(job));
+    job.frames = (const DgFrameDev*)c->d_stage[slot];
+    job.segs = (const DgSegDev*)((uint8_t*)c->d_stage[slot] + fbytes);
+    job.nframes = n;
+    job.nsegs = (uint32_t)segs.size();
+    job.total_vtx = (uint32_t)total_vtx;
+    job.total_tri = (uint32_t)total_tri;
+    job.total_tiles = (uint32_t)total_tiles;
+    job.shade_stride = stride;
+    job.vrec = c->d_vrec;
+    job.vshade = c->d_vshade;
+    job.large = c->d_large;
+    job.large_base = c->d_large_base;
+    job.large_cap = (uint32_t)std::min<size_t>(c->large_cap, (1u << 24) - 1);
+    job.large_counter = c->d_counters;
+    job.stats = c->d_counters + 1;
+    job.tex = c->d_tex;
+    job.err = c->d_err;
+    c->last_vtx = total_vtx;
+    c->last_tri = total_tri;
+
+    DG_CUDA(cudaMemsetAsync(c->d_counters, 0, 3 * sizeof(unsigned long long), c->stream));
+    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[0], c->stream));
+    DG_CUDA(dg_launch_vertex(job, c->stream));
+    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    DG_CUDA(dg_launch_setup_raster(job, c->nsm, c->stream));
+    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[2], c->stream));
+    DG_CUDA(dg_launch_large_raster(job, c->nsm, c->stream));
+    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[3], c->stream));
+    DG_CUDA(dg_launch_resolve(job, c->stream));
+    if (c->timing) {
+        DG_CUDA(cudaEventRecord(c->ev[4], c->stream));
+        c->ev_valid = true;
+    }
+    return DG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dg_status_string(dg_status s) {
+    switch (s) {
+        case DG_OK: return "ok";
+        case DG_E_INVALID: return "invalid argument";
+        case DG_E_INDEX: return "mesh index out of range";
+        case DG_E_TEXTURE_RANGE: return "texel offset outside the texture map";
+        case DG_E_CAMERA: return "camera or view-plane assertion failed";
+        case DG_E_DEPTH_UNINIT: return "canvas depth buffer not initialized";
+        case DG_E_CUDA: return "CUDA error";
+        case DG_E_OOM: return "out of device memory";
+        case DG_E_LIMIT: return "size or feature beyond a documented limit";
+        case DG_E_TIMEOUT: return "bounded wait timed out";
+        default: return "unknown status";
+    }
+}
+
+dg_status dg_ctx_create(int32_t device, dg_ctx** out) {
+    if (!out) return DG_E_INVALID;
+    *out = nullptr;
+    if (device == -1) {  // host-only context: scenes and cameras work, device calls return DG_E_CUDA
+        dg_ctx* h = new (std::nothrow) dg_ctx();
+        if (!h) return DG_E_OOM;
+        h->device = -1;
+        *out = h;
+        return DG_OK;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return DG_E_CUDA;
+    }
+    std::unique_ptr<dg_ctx> c(new (std::nothrow) dg_ctx());
+    if (!c) return DG_E_OOM;
+    c->device = device;
+    DG_CUDA(cudaSetDevice(device));
+    DG_CUDA(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+    DG_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+    c->stream = c->own_stream;
+    for (int i = 0; i < dg_ctx::kSlots; i++) DG_CUDA(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming));
+    for (int i = 0; i < 5; i++) DG_CUDA(cudaEventCreate(&c->ev[i]));
+    dg_status e = dalloc(&c->d_counters, 4);
+    if (e) return e;
+    e = dalloc(&c->d_err, 1);
+    if (e) return e;
+    DG_CUDA(cudaMemset(c->d_err, 0, 4));
+    TexMap white;
+    const uint8_t px[3] = {255, 255, 255};  // TextureMap::default, scene/mod.rs:128-135
+    e = tex_upload(c.get(), px, 3, 1, 1, 3, white);
+    if (e) return e;
+    c->tex.push_back(white);
+    *out = c.release();
+    return DG_OK;
+}
+
+dg_status dg_ctx_destroy(dg_ctx* c) {
+    if (!c) return DG_E_INVALID;
+    if (c->device < 0) {
+        delete c;
+        return DG_OK;
+    }
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& t : c->tex) dfree(t.d_words);
+    for (auto& o : c->objects) {
+        dfree(o.d_pos); dfree(o.d_nrm); dfree(o.d_uv);
+        dfree(o.d_tri_pos); dfree(o.d_tri_uv); dfree(o.d_tri_nrm); dfree(o.d_mats);
+    }
+    for (auto& v : c->canvases) {
+        dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
+    }
+    dfree(c->d_tex); dfree(c->d_vrec); dfree(c->d_vshade); dfree(c->d_large); dfree(c->d_large_base);
+    dfree(c->d_counters); dfree(c->d_err);
+    for (int i = 0; i < dg_ctx::kSlots; i++) {
+        if (c->h_stage[i]) cudaFreeHost(c->h_stage[i]);
+        dfree(c->d_stage[i]);
+        if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
+    }
+    for (int i = 0; i < 5; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return DG_OK;
+}
+
+dg_status dg_ctx_synchronize(dg_ctx* c) {
+    if (!c) return DG_E_INVALID;
+    dg_status e = set_device(c);
+    if (e) return e;
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    return take_errors(c);
+}
+
+dg_status dg_ctx_set_stream(dg_ctx* c, void* stream) {
+    if (!c) return DG_E_INVALID;
+    if (c->device < 0) return DG_E_CUDA;
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return DG_OK;
+}
+
+void* dg_ctx_stream(dg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+dg_status dg_ctx_set_timing(dg_ctx* c, int32_t enable) {
+    if (!c) return DG_E_INVALID;
+    c->timing = enable != 0;
+    c->ev_valid = false;
+    return DG_OK;
+}
+
+dg_status dg_ctx_kernel_times(dg_ctx* c, float* ms, int32_t n) {
+    if (!c || !ms || n < 0) return DG_E_INVALID;
+    if (c->device < 0) return DG_E_CUDA;
+    if (!c->ev_valid) return DG_E_INVALID;
+    DG_CUDA(cudaEventSynchronize(c->ev[4]));
+    for (int i = 0; i < n && i < 4; i++) DG_CUDA(cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]));
+    return DG_OK;
+}
+
+dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
+    if (!c || !out || n < 0) return DG_E_INVALID;
+    if (c->device < 0) return DG_E_CUDA;
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    unsigned long long h[3];
+    DG_CUDA(cudaMemcpy(h, c->d_counters, sizeof(h), cudaMemcpyDeviceToHost));
+    uint64_t v[6] = {c->last_vtx, c->last_tri, h[0] >> DG_PACK_SHIFT, h[0] & ((1ull << DG_PACK_SHIFT) - 1ull), h[1], h[2]};
+    for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+    return DG_OK;
+}
+
+dg_status dg_texmap_create(dg_ctx* c, const uint8_t* img, uint64_t len, uint64_t w, uint64_t h, uint64_t comps,
+                           int32_t* out_id) {
+    if (!c || !out_id || (len && !img)) return DG_E_INVALID;
+    // scene/mod.rs:114-115
+    if (comps == 0 || len % comps != 0 || len / comps != w * h) return DG_E_INVALID;
+    if (w > 0xFFFFFFFFull || h > 0xFFFFFFFFull || comps > 0xFFFFFFFFull) return DG_E_LIMIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    TexMap t;
+    e = tex_upload(c, img, len, (uint32_t)w, (uint32_t)h, (uint32_t)comps, t);
+    if (e) return e;
+    c->tex.push_back(t);
+    c->tex_dirty = true;
+    *out_id = (int32_t)c->tex.size() - 2;  // user ids start at 0; [0] is the default map
+    return DG_OK;
+}
+
+dg_status dg_object_create(dg_ctx* c, const float* vertices, uint64_t nv, const float* normals, uint64_t nn,
+                           const float* uvs, uint64_t nuv, const dg_mesh_desc* meshes, uint64_t nmesh,
+                           const dg_material* mats, uint64_t nmat, int32_t* out_id) {
+    if (!c || !out_id) return DG_E_INVALID;
+    if ((nv && !vertices) || (nn && !normals) || (nuv && !uvs) || (nmesh && !meshes) || (nmat && !mats))
+        return DG_E_INVALID;
+    if (nv >= 0xFFFFFFFFull || nn >= 0xFFFFFFFFull || nuv >= 0xFFFFFFFFull) return DG_E_LIMIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    std::vector<DgMatDev> dm(nmat);
+    for (uint64_t i = 0; i < nmat; i++) {
+        for (int k = 0; k < 3; k++) {
+            dm[i].ka[k] = mats[i].ka[k];
+            dm[i].kd[k] = mats[i].kd[k];
+            dm[i].ks[k] = mats[i].ks[k];
+        }
+        dm[i].alpha = mats[i].alpha;
+        int32_t ids[2] = {mats[i].map_ka, mats[i].map_kd};
+        uint32_t tix[2];
+        for (int k = 0; k < 2; k++) {
+            if (ids[k] < -1 || ids[k] + 1 >= (int64_t)c->tex.size()) return DG_E_INVALID;
+            tix[k] = (uint32_t)(ids[k] + 1);
+        }
+        dm[i].map_ka = tix[0];
+        dm[i].map_kd = tix[1];
+    }
+    Object o;
+    std::vector<uint4> tpos, tuv, tnrm;
+    uint64_t total = 0;
+    for (uint64_t m = 0; m < nmesh; m++) {
+        if (meshes[m].ntri && !meshes[m].tris) return DG_E_INVALID;
+        // object.rs:46-53: textures[texture_idx] panics when out of range
+        if (meshes[m].texture_idx < 0 || (uint64_t)meshes[m].texture_idx >= nmat) return DG_E_INVALID;
+        total += meshes[m].ntri;
+        for (uint64_t t = 0; t < meshes[m].ntri; t++) {
+            const uint32_t* q = meshes[m].tris + 9 * t;
+            for (int k = 0; k < 3; k++)  // mesh.rs:46-48
+                if (q[k] >= nv || q[3 + k] >= nuv || q[6 + k] >= nn) return DG_E_INDEX;
+        }
+    }
+    if (total >= (1ull << 30)) return DG_E_LIMIT;
+    for (uint64_t m = 0; m < nmesh; m++) {
+        const dg_mesh_desc& md = meshes[m];
+        bool transparent = mats[md.texture_idx].alpha < 1.0f;
+        if (transparent) {
+            o.transparent.emplace_back(md.tris, md.tris + 9 * md.ntri);
+            o.transparent_mat.push_back(md.texture_idx);
+            continue;
+        }
+        for (uint64_t t = 0; t < md.ntri; t++) {
+            const uint32_t* q = md.tris + 9 * t;
+            tpos.push_back(make_uint4(q[0], q[1], q[2], (uint32_t)md.texture_idx));
+            tuv.push_back(make_uint4(q[3], q[4], q[5], 0u));
+            tnrm.push_back(make_uint4(q[6], q[7], q[8], 0u));
+        }
+    }
+    std::vector<float4> p4(nv), n4(nn);
+    std::vector<float2> u2(nuv);
+    for (uint64_t i = 0; i < nv; i++) p4[i] = make_float4(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2], 1.0f);
+    for (uint64_t i = 0; i < nn; i++) n4[i] = make_float4(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2], 0.0f);
+    for (uint64_t i = 0; i < nuv; i++) u2[i] = make_float2(uvs[3 * i], uvs[3 * i + 1]);
+    o.h_pos.assign(vertices, vertices + 3 * nv);
+    o.nv = (uint32_t)nv;
+    o.nn = (uint32_t)nn;
+    o.nuv = (uint32_t)nuv;
+    o.ntri_opaque = (uint32_t)tpos.size();
+    o.nmats = (uint32_t)nmat;
+    auto up = [&](auto** dst, const auto& src) -> dg_status {
+        dg_status ee = dalloc(dst, src.size());
+        if (ee) return ee;
+        if (!src.empty())
+            DG_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice));
+        return DG_OK;
+    };
+    if ((e = up(&o.d_pos, p4)) || (e = up(&o.d_nrm, n4)) || (e = up(&o.d_uv, u2)) || (e = up(&o.d_tri_pos, tpos)) ||
+        (e = up(&o.d_tri_uv, tuv)) || (e = up(&o.d_tri_nrm, tnrm)) || (e = up(&o.d_mats, dm))) {
+        dfree(o.d_pos); dfree(o.d_nrm); dfree(o.d_uv);
+        dfree(o.d_tri_pos); dfree(o.d_tri_uv); dfree(o.d_tri_nrm); dfree(o.d_mats);
+        return e;
+    }
+    o.alive = true;
+    c->objects.push_back(std::move(o));
+    *out_id = (int32_t)c->objects.size() - 1;
+    return DG_OK;
+}
+
+dg_status dg_object_destroy(dg_ctx* c, int32_t id) {
+    Object* o = get_object(c, id);
+    if (!o) return DG_E_INVALID;
+    for (auto& s : c->scenes)
+        for (int32_t x : s.objects)
+            if (x == id) return DG_E_INVALID;  // still referenced by a scene
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    dfree(o->d_pos); dfree(o->d_nrm); dfree(o->d_uv);
+    dfree(o->d_tri_pos); dfree(o->d_tri_uv); dfree(o->d_tri_nrm); dfree(o->d_mats);
+    o->alive = false;
+    return DG_OK;
+}
+
+dg_status dg_scene_create(dg_ctx* c, uint64_t width, uint64_t height, int32_t* out_id) {
+    if (!c || !out_id || width == 0 || height == 0) return DG_E_INVALID;
+    Scene s;
+    s.width = width;
+    s.height = height;
+    HV3 pos = h3(0.0f, 0.0f, 150.0f);  // scene/mod.rs:763-769
+    HV3 dir = hmul(pos, -1.0f);
+    s.lights.push_back(h3(0.0f, 300.0f, 300.0f));
+    s.exponent = 2;
+    float ratio = (float)width / (float)height;
+    dg_status e = camera_init(s.cam, pos, dir, ratio, -10.0f, -10.0f - 500.0f, 135.0f);
+    if (e) return e;
+    c->scenes.push_back(s);
+    *out_id = (int32_t)c->scenes.size() - 1;
+    return DG_OK;
+}
+
+dg_status dg_scene_add_obj(dg_ctx* c, int32_t scene, int32_t object, uint32_t* out_obj_id) {
+    Scene* s = get_scene(c, scene);
+    if (!s || !get_object(c, object)) return DG_E_INVALID;
+    s->objects.push_back(object);
+    if (out_obj_id) *out_obj_id = (uint32_t)s->objects.size() - 1;
+    return DG_OK;
+}
+
+dg_status dg_scene_set_camera(dg_ctx* c, int32_t scene, const float pos[3], const float dir[3], float ratio,
+                              float near_, float far_, float fov_x_deg) {
+    Scene* s = get_scene(c, scene);
+    if (!s || !pos || !dir) return DG_E_INVALID;
+    return camera_init(s->cam, h3(pos[0], pos[1], pos[2]), h3(dir[0], dir[1], dir[2]), ratio, near_, far_, fov_x_deg);
+}
+
+dg_status dg_scene_camera_op(dg_ctx* c, int32_t scene, int32_t op, const float* a) {
+    Scene* s = get_scene(c, scene);
+    if (!s || !a) return DG_E_INVALID;
+    Camera& cam = s->cam;
+    switch (op) {
+        case 0: cam.position = hadd(cam.position, hmul(cam.up, a[0])); break;     // move_up
+        case 1: cam.position = hadd(cam.position, hmul(cam.up, -a[0])); break;    // move_down
+        case 2: cam.position = hadd(cam.position, hmul(cam.u, -a[0])); break;     // move_left
+        case 3: cam.position = hadd(cam.position, hmul(cam.u, a[0])); break;      // move_right
+        case 4: cam.position = hadd(cam.position, hmul(hnormalized(hcross(cam.up, cam.u)), a[0])); break;
+        case 5: cam.position = hadd(cam.position, hmul(hnormalized(hcross(cam.u, cam.up)), a[0])); break;
+        case 6: {  // rotate_origin: Matrix4::rotate_y(theta.to_radians()) * v.as_vec4()
+            float th = a[0] * kRadsPerDeg;
+            float sn = std::sin(th), cs = std::cos(th);
+            HM4 r = hm_zero();
+            r.m[0][0] = cs; r.m[0][2] = sn; r.m[1][1] = 1.0f; r.m[2][0] = -sn; r.m[2][2] = cs; r.m[3][3] = 1.0f;
+            float p[4] = {cam.position.x, cam.position.y, cam.position.z, 1.0f}, po[4];
+            float d[4] = {cam.direction.x, cam.direction.y, cam.direction.z, 1.0f}, dout[4];
+            hm_vec(r, p, po);
+            hm_vec(r, d, dout);
+            cam.position = h3(po[0], po[1], po[2]);
+            cam.direction = h3(dout[0], dout[1], dout[2]);
+            break;
+        }
+        case 7: cam.position = h3(a[0], a[1], a[2]); break;
+        case 8: {  // Scene::move_camera_direction
+            int32_t dx = (int32_t)a[0], dy = (int32_t)a[1];
+            if (!((int64_t)dx < (int64_t)s->width) || !((int64_t)dy < (int64_t)s->height)) return DG_E_INVALID;
+            float fx = (float)dx / (float)s->width, fy = (float)dy / (float)s->height;
+            cam.direction = hnormalized(hadd(hadd(cam.direction, hmul(cam.u, fx)), hmul(cam.v, fy)));
+            camera_update_basis(cam);
+            break;
+        }
+        default: return DG_E_INVALID;
+    }
+    return DG_OK;
+}
+
+dg_status dg_scene_get_camera(dg_ctx* c, int32_t scene, float pos[3], float dir[3]) {
+    Scene* s = get_scene(c, scene);
+    if (!s || !pos || !dir) return DG_E_INVALID;
+    pos[0] = s->cam.position.x; pos[1] = s->cam.position.y; pos[2] = s->cam.position.z;
+    dir[0] = s->cam.direction.x; dir[1] = s->cam.direction.y; dir[2] = s->cam.direction.z;
+    return DG_OK;
+}
+
+dg_status dg_scene_set_lights(dg_ctx* c, int32_t scene, const float* pos, uint32_t n) {
+    Scene* s = get_scene(c, scene);
+    if (!s || !pos || n == 0 || n > DG_MAX_LIGHTS) return DG_E_INVALID;
+    s->lights.clear();
+    for (uint32_t i = 0; i < n; i++) s->lights.push_back(h3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    return DG_OK;
+}
+
+dg_status dg_scene_set_exponent(dg_ctx* c, int32_t scene, int32_t exponent) {
+    Scene* s = get_scene(c, scene);
+    if (!s) return DG_E_INVALID;
+    s->exponent = exponent;
+    return DG_OK;
+}
+
+dg_status dg_scene_frame_setup(dg_ctx* c, int32_t scene, float M[16], float planes[24]) {
+    Scene* s = get_scene(c, scene);
+    if (!s || !M || !planes) return DG_E_INVALID;
+    float m[4][4], p[6][4];
+    dg_status e = frame_setup(*s, m, p);
+    if (e) return e;
+    std::memcpy(M, m, sizeof(m));
+    std::memcpy(planes, p, sizeof(p));
+    return DG_OK;
+}
+
+dg_status dg_object_transparent_tris(dg_ctx* c, int32_t object, uint32_t mesh, uint32_t* out, uint64_t cap,
+                                     uint64_t* out_ntri) {
+    Object* o = get_object(c, object);
+    if (!o || mesh >= o->transparent.size()) return DG_E_INVALID;
+    const auto& t = o->transparent[mesh];
+    if (out_ntri) *out_ntri = t.size() / 9;
+    if (out) {
+        if (cap < t.size()) return DG_E_INVALID;
+        std::memcpy(out, t.data(), t.size() * 4);
+    }
+    return DG_OK;
+}
+
+dg_status dg_canvas_create(dg_ctx* c, uint64_t width, uint64_t height, int32_t* out_id) {
+    if (!c || !out_id || width == 0 || height == 0) return DG_E_INVALID;
+    if (width > 65535 || height > 65535) return DG_E_LIMIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    Canvas v;
+    uint64_t n = width * height;
+    if ((e = dalloc(&v.d_colour, n)) || (e = dalloc(&v.d_depth, n)) || (e = dalloc(&v.d_vis, n))) {
+        dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
+        return e;
+    }
+    v.w = width;
+    v.h = height;
+    // Canvas::new: black frame (canvas.rs:368), no depth buffer yet
+    DG_CUDA(dg_launch_fill(v.d_colour, v.d_depth, n, 0xFF000000u, 0.0f, 1, 0, c->stream));
+    DG_CUDA(dg_launch_vis_reset(v.d_vis, n, c->stream));
+    v.alive = true;
+    c->canvases.push_back(v);
+    *out_id = (int32_t)c->canvases.size() - 1;
+    return DG_OK;
+}
+
+dg_status dg_canvas_destroy(dg_ctx* c, int32_t id) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis);
+    v->alive = false;
+    return DG_OK;
+}
+
+dg_status dg_canvas_init_depth(dg_ctx* c, int32_t id, float depth) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    dg_status e = set_device(c);
+    if (e) return e;
+    v->depth_max = depth;
+    v->depth_init = true;
+    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, v->w * v->h, 0u, depth, 0, 1, c->stream));
+    return DG_OK;
+}
+
+dg_status dg_canvas_apply_offset(dg_ctx* c, int32_t id, int32_t x, int32_t y) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    v->off_x = (float)x;
+    v->off_y = (float)y;
+    return DG_OK;
+}
+
+dg_status dg_canvas_resize(dg_ctx* c, int32_t id, uint64_t width, uint64_t height) {
+    Canvas* v = get_canvas(c, id);
+    if (!v || width == 0 || height == 0) return DG_E_INVALID;
+    if (width > 65535 || height > 65535) return DG_E_LIMIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    uint64_t n_old = v->w * v->h, n = width * height;
+    // Vec::resize keeps the first min(old, new) pixels and pads with black (canvas.rs:390)
+    uint32_t* col = nullptr;
+    float* dep = nullptr;
+    uint64_t* vis = nullptr;
+    if ((e = dalloc(&col, n)) || (e = dalloc(&dep, n)) || (e = dalloc(&vis, n))) {
+        dfree(col); dfree(dep); dfree(vis);
+        return e;
+    }
+    DG_CUDA(dg_launch_fill(col, dep, n, 0xFF000000u, 0.0f, 1, 0, c->stream));
+    DG_CUDA(cudaMemcpyAsync(col, v->d_colour, std::min(n, n_old) * 4, cudaMemcpyDeviceToDevice, c->stream));
+    DG_CUDA(dg_launch_vis_reset(vis, n, c->stream));
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis);
+    v->d_colour = col;
+    v->d_depth = dep;
+    v->d_vis = vis;
+    v->w = width;
+    v->h = height;
+    // init_depth(depth_max) (canvas.rs:392)
+    v->depth_init = true;
+    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, n, 0u, v->depth_max, 0, 1, c->stream));
+    return DG_OK;
+}
+
+dg_status dg_canvas_clear(dg_ctx* c, int32_t id) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    dg_status e = set_device(c);
+    if (e) return e;
+    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, v->w * v->h, 0xFF9BBAFFu, v->depth_max, 1, v->depth_init ? 1 : 0,
+                           c->stream));
+    return DG_OK;
+}
+
+dg_status dg_canvas_read(dg_ctx* c, int32_t id, uint8_t* bgra, float* depth) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    if (depth && !v->depth_init) return DG_E_DEPTH_UNINIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    uint64_t n = v->w * v->h;
+    if (bgra) DG_CUDA(cudaMemcpyAsync(bgra, v->d_colour, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (depth) DG_CUDA(cudaMemcpyAsync(depth, v->d_depth, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    return take_errors(c);
+}
+
+dg_status dg_canvas_write(dg_ctx* c, int32_t id, const uint8_t* bgra, const float* depth) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    if (depth && !v->depth_init) return DG_E_DEPTH_UNINIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    uint64_t n = v->w * v->h;
+    if (bgra) DG_CUDA(cudaMemcpyAsync(v->d_colour, bgra, n * 4, cudaMemcpyHostToDevice, c->stream));
+    if (depth) DG_CUDA(cudaMemcpyAsync(v->d_depth, depth, n * 4, cudaMemcpyHostToDevice, c->stream));
+    DG_CUDA(cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+dg_status dg_canvas_device_ptrs(dg_ctx* c, int32_t id, void** bgra, void** depth) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    if (bgra) *bgra = v->d_colour;
+    if (depth) *depth = v->d_depth;
+    return DG_OK;
+}
+
+dg_status dg_canvas_size(dg_ctx* c, int32_t id, uint64_t* w, uint64_t* h) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    if (w) *w = v->w;
+    if (h) *h = v->h;
+    return DG_OK;
+}
+
+dg_status dg_scene_render(dg_ctx* c, int32_t scene, int32_t canvas) {
+    if (!c) return DG_E_INVALID;
+    return render_job(c, &scene, &canvas, 1);
+}
+
+dg_status dg_render_batch(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n) {
+    if (!c || (n && (!scenes || !canvases))) return DG_E_INVALID;
+    return render_job(c, scenes, canvases, n);
+}
+
+}  // extern "C"

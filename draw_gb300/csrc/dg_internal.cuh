@@ -1,0 +1,120 @@
+// dg_internal.cuh -- device-side data layout shared by the host API (dg_api.cu)
+// and the kernels (dg_kernels.cu) of the GB300 rasterizer.
+//
+// HBM layout (all resident until their owner is destroyed):
+//   texture map   : image bytes packed into u32 words (+1 pad word), row 0 = top
+//   object        : pos float4[V] (w = 1), nrm float4[N], uv float2[U],
+//                   tri_pos uint4[T] = (p0,p1,p2,material), tri_uv uint4[T],
+//                   tri_nrm uint4[T]; opaque meshes first, in submission order
+//   canvas        : colour u32[W*H] (BGRA bytes, row 0 = top), depth f32[W*H]
+//                   (y*W+x, y = 0 at the bottom), vis u64[W*H] (visibility keys,
+//                   kept at DG_VIS_EMPTY between frames)
+//   render scratch: vrec float4[V_total] (snapped centre x,y, eye distance,
+//                   plane-sign masks), vshade float4[V_total*L*2] (light, halfway),
+//                   large-triangle records + their block bases, counters
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/draw_gpu.h"
+
+#define DG_MAXL DG_MAX_LIGHTS
+#define DG_VIS_EMPTY 0xFFFFFFFFFFFFFFFFull
+
+// Triangles whose clipped bounding box has more pixels than this go to the
+// large-triangle pass (8x8 pixel blocks spread over all warps).
+#define DG_SMALL_MAX_PX 1024u
+#define DG_BLOCK 8u
+// Resolve tile: 32 x 8 pixels, one CTA of 256 threads.
+#define DG_TILE_W 32u
+#define DG_TILE_H 8u
+#define DG_PACK_SHIFT 40
+
+struct DgTexDev {
+    const uint32_t* words;  // image bytes, little-endian in u32 words, one pad word at the end
+    uint64_t len;           // image length in bytes
+    uint32_t width, height, comps;
+    float fw, fh;           // width as f32, height as f32
+};
+
+struct DgMatDev {
+    float ka[3], kd[3], ks[3];
+    float alpha;
+    uint32_t map_ka, map_kd;  // indices into the context's texture table
+};
+
+// One frame of a render job (a (scene, canvas) pair).
+struct DgFrameDev {
+    float M[4][4];       // viewport * orth * persp * view
+    float plane[6][4];   // near, far, right, left, top, bottom: (n.x, n.y, n.z, k)
+    float cam[3];
+    float clear_depth;   // Canvas::depth_max
+    float light[DG_MAXL][3];
+    uint32_t nlights;
+    int32_t exponent;
+    float off_x, off_y;  // Canvas::offset
+    uint32_t width, height;
+    uint64_t* vis;
+    uint32_t* colour;
+    float* depth;
+    uint32_t seg_begin, seg_count;  // this frame's segments (ascending seq_base)
+    uint32_t tile_begin, tiles_x;   // this frame's resolve tiles
+    uint32_t pad[2];
+};
+
+// The opaque triangles and the vertices of one object within one frame.
+struct DgSegDev {
+    uint32_t frame;
+    uint32_t tri_begin;  // job-wide index of the segment's first triangle
+    uint32_t vtx_begin;  // job-wide index of the segment's first vertex (vrec/vshade row)
+    uint32_t seq_base;   // frame-local submission index of the first triangle
+    uint32_t ntri, nv;
+    uint32_t nmats, pad;
+    const float4* pos;
+    const float4* nrm;
+    const float2* uv;
+    const uint4* tri_pos;
+    const uint4* tri_uv;
+    const uint4* tri_nrm;
+    const DgMatDev* mats;
+};
+
+// A triangle with too many bounding-box pixels for the warp-flattened path.
+struct DgLargeRec {
+    float ax, ay, bx, by, cx, cy;  // snapped centres
+    float da, db, dc;              // vertex depths
+    uint32_t seq;                  // frame-local key low word
+    uint32_t frame;
+    uint32_t xlo, ylo, xhi, yhi;
+    uint32_t bw;       // blocks per row
+    uint32_t nblocks;
+    uint32_t pad[3];
+};
+
+struct DgJobDev {
+    const DgFrameDev* frames;
+    const DgSegDev* segs;
+    uint32_t nframes, nsegs;
+    uint32_t total_vtx, total_tri, total_tiles;
+    uint32_t shade_stride;  // lights per vertex row of vshade (max over frames)
+    float4* vrec;
+    float4* vshade;
+    DgLargeRec* large;
+    uint32_t* large_base;   // block base of each record (ascending)
+    uint32_t large_cap;
+    uint32_t pad0;
+    unsigned long long* large_counter;  // (records << 40) | blocks
+    unsigned long long* stats;          // [0] covered pixels, [1] overflowed large triangles
+    const DgTexDev* tex;
+    uint32_t* err;
+};
+
+// Host-side launchers (dg_kernels.cu).
+cudaError_t dg_launch_vertex(const DgJobDev& job, cudaStream_t s);
+cudaError_t dg_launch_setup_raster(const DgJobDev& job, int nsm, cudaStream_t s);
+cudaError_t dg_launch_large_raster(const DgJobDev& job, int nsm, cudaStream_t s);
+cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s);
+cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,
+                           int fill_colour, int fill_depth, cudaStream_t s);
+cudaError_t dg_launch_vis_reset(uint64_t* vis, uint64_t n, cudaStream_t s);

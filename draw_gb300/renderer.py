@@ -1,0 +1,425 @@
+"""Python mirror of the reference renderer's object model over the C ABI.
+
+The reference (mororo18/draw, Rust) exposes ``Scene``, ``Camera``, ``Object``,
+``Texture``, ``TextureMap`` and ``Canvas`` (src/renderer/scene/mod.rs,
+scene/object.rs, canvas.rs). The classes here keep those names, argument
+meanings and method names, and call the CUDA library ``libdrawgpu.so``
+(include/draw_gpu.h) through ctypes. Where the reference panics (assert!,
+unwrap, out-of-range slice), these raise ``DrawError`` carrying the library's
+status code. There is no CPU fallback: importing this module on a machine
+without the built library or without a GPU fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libdrawgpu.so")
+
+DG_OK = 0
+STATUS = {
+    1: "DG_E_INVALID", 2: "DG_E_INDEX", 3: "DG_E_TEXTURE_RANGE", 4: "DG_E_CAMERA", 5: "DG_E_DEPTH_UNINIT",
+    6: "DG_E_CUDA", 7: "DG_E_OOM", 8: "DG_E_LIMIT", 9: "DG_E_TIMEOUT",
+}
+
+# Every symbol declared in include/draw_gpu.h, with its ctypes signature.
+_P, _i32, _u32, _u64, _f32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float
+SIGNATURES = {
+    "dg_ctx_create": (_i32, [_i32, _P]),
+    "dg_ctx_destroy": (_i32, [_P]),
+    "dg_status_string": (ctypes.c_char_p, [_i32]),
+    "dg_ctx_synchronize": (_i32, [_P]),
+    "dg_ctx_set_stream": (_i32, [_P, _P]),
+    "dg_ctx_stream": (_P, [_P]),
+    "dg_ctx_set_timing": (_i32, [_P, _i32]),
+    "dg_ctx_kernel_times": (_i32, [_P, _P, _i32]),
+    "dg_ctx_last_stats": (_i32, [_P, _P, _i32]),
+    "dg_texmap_create": (_i32, [_P, _P, _u64, _u64, _u64, _u64, _P]),
+    "dg_object_create": (_i32, [_P, _P, _u64, _P, _u64, _P, _u64, _P, _u64, _P, _u64, _P]),
+    "dg_object_destroy": (_i32, [_P, _i32]),
+    "dg_scene_create": (_i32, [_P, _u64, _u64, _P]),
+    "dg_scene_add_obj": (_i32, [_P, _i32, _i32, _P]),
+    "dg_scene_set_camera": (_i32, [_P, _i32, _P, _P, _f32, _f32, _f32, _f32]),
+    "dg_scene_camera_op": (_i32, [_P, _i32, _i32, _P]),
+    "dg_scene_get_camera": (_i32, [_P, _i32, _P, _P]),
+    "dg_scene_set_lights": (_i32, [_P, _i32, _P, _u32]),
+    "dg_scene_set_exponent": (_i32, [_P, _i32, _i32]),
+    "dg_scene_frame_setup": (_i32, [_P, _i32, _P, _P]),
+    "dg_object_transparent_tris": (_i32, [_P, _i32, _u32, _P, _u64, _P]),
+    "dg_canvas_create": (_i32, [_P, _u64, _u64, _P]),
+    "dg_canvas_destroy": (_i32, [_P, _i32]),
+    "dg_canvas_init_depth": (_i32, [_P, _i32, _f32]),
+    "dg_canvas_apply_offset": (_i32, [_P, _i32, _i32, _i32]),
+    "dg_canvas_resize": (_i32, [_P, _i32, _u64, _u64]),
+    "dg_canvas_clear": (_i32, [_P, _i32]),
+    "dg_canvas_read": (_i32, [_P, _i32, _P, _P]),
+    "dg_canvas_write": (_i32, [_P, _i32, _P, _P]),
+    "dg_canvas_device_ptrs": (_i32, [_P, _i32, _P, _P]),
+    "dg_canvas_size": (_i32, [_P, _i32, _P, _P]),
+    "dg_scene_render": (_i32, [_P, _i32, _i32]),
+    "dg_render_batch": (_i32, [_P, _P, _P, _u32]),
+}
+
+
+class DrawError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        super().__init__(f"{what}: {STATUS.get(status, status)}")
+        self.status = status
+
+
+class dg_material(ctypes.Structure):
+    _fields_ = [("ka", ctypes.c_float * 3), ("kd", ctypes.c_float * 3), ("ks", ctypes.c_float * 3),
+                ("alpha", ctypes.c_float), ("map_ka", ctypes.c_int32), ("map_kd", ctypes.c_int32)]
+
+
+class dg_mesh_desc(ctypes.Structure):
+    _fields_ = [("tris", ctypes.c_void_p), ("ntri", ctypes.c_uint64), ("texture_idx", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads the in-tree libdrawgpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with draw_gb300._build.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _chk(st: int, what: str):
+    if st != DG_OK:
+        raise DrawError(st, what)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    """One CUDA device and stream; owns every resource created through it."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        _chk(self.lib.dg_ctx_create(device, ctypes.byref(h)), "dg_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.dg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def synchronize(self):
+        _chk(self.lib.dg_ctx_synchronize(self.h), "synchronize")
+
+    def set_stream(self, stream_ptr: int | None):
+        _chk(self.lib.dg_ctx_set_stream(self.h, stream_ptr), "set_stream")
+
+    def set_timing(self, on: bool):
+        _chk(self.lib.dg_ctx_set_timing(self.h, 1 if on else 0), "set_timing")
+
+    def kernel_times(self) -> dict:
+        ms = (ctypes.c_float * 4)()
+        _chk(self.lib.dg_ctx_kernel_times(self.h, ms, 4), "kernel_times")
+        return dict(zip(["vertex", "setup_raster", "large_raster", "resolve"], list(ms)))
+
+    def last_stats(self) -> dict:
+        v = (ctypes.c_uint64 * 6)()
+        _chk(self.lib.dg_ctx_last_stats(self.h, v, 6), "last_stats")
+        keys = ["vertices", "triangles", "large_triangles", "large_blocks", "covered_pixels", "large_overflow"]
+        return dict(zip(keys, list(v)))
+
+    def render_batch(self, scenes: list, canvases: list):
+        """The batched form: all frames in one launch per pipeline stage."""
+        s = np.array([x.id for x in scenes], np.int32)
+        c = np.array([x.id for x in canvases], np.int32)
+        _chk(self.lib.dg_render_batch(self.h, _ptr(s), _ptr(c), len(scenes)), "render_batch")
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class TextureMap:
+    """TextureMap::new(img, width, height, components), scene/mod.rs:113-126."""
+
+    def __init__(self, img, width: int, height: int, components: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        a = np.ascontiguousarray(img, dtype=np.uint8).reshape(-1)
+        out = ctypes.c_int32()
+        _chk(self.ctx.lib.dg_texmap_create(self.ctx.h, _ptr(a), a.size, width, height, components,
+                                           ctypes.byref(out)), "TextureMap::new")
+        self.id = out.value
+        self.width, self.height, self.components = width, height, components
+
+
+@dataclass
+class Texture:
+    """The reference's material (scene/mod.rs:206-216); map_* = TextureMap or None
+    for the 1x1 white default map."""
+
+    name: str = "default"
+    ka: tuple = (0.9, 0.9, 0.9)
+    kd: tuple = (0.4, 0.4, 0.4)
+    ks: tuple = (0.5, 0.5, 0.5)
+    alpha: float = 1.0
+    map_ka: TextureMap | None = None
+    map_kd: TextureMap | None = None
+
+    @staticmethod
+    def default() -> "Texture":  # scene/mod.rs:237-252
+        return Texture()
+
+    @staticmethod
+    def with_diffuse_map(diff_map: TextureMap) -> "Texture":  # scene/mod.rs:219-234
+        return Texture("default", (1.0, 1.0, 1.0), (1.0, 1.0, 1.0), (1.0, 1.0, 1.0), 1.0, None, diff_map)
+
+
+@dataclass
+class IndexedMesh:
+    """scene/mesh.rs:30-35: triangles as (T, 9) indices (position[3], texture[3], normal[3])."""
+
+    name: str
+    triangles: np.ndarray
+    texture_idx: int = 0
+
+
+@dataclass
+class MeshInfo:
+    name: str
+    triangle_count: int
+    texture_name: str | None
+
+
+@dataclass
+class ObjectInfo:
+    id: int
+    name: str
+    mesh_info_list: list = field(default_factory=list)
+
+
+class Object:
+    """Object::new(name, vertices, normals, texture_vertices, meshes, textures), object.rs:34-71."""
+
+    def __init__(self, name: str, vertices, normals, texture_vertices, meshes: list, textures: list,
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.name = name
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        uv = np.asarray(texture_vertices if texture_vertices is not None else np.zeros((0, 3)), np.float32)
+        if uv.ndim == 2 and uv.shape[1] == 2:
+            uv = np.concatenate([uv, np.zeros((uv.shape[0], 1), np.float32)], 1)
+        uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 3)
+        tris = [np.ascontiguousarray(m.triangles, np.uint32).reshape(-1, 9) for m in meshes]
+        md = (dg_mesh_desc * max(1, len(meshes)))()
+        for i, (m, t) in enumerate(zip(meshes, tris)):
+            md[i].tris = t.ctypes.data_as(ctypes.c_void_p)
+            md[i].ntri = t.shape[0]
+            md[i].texture_idx = m.texture_idx
+        mats = (dg_material * max(1, len(textures)))()
+        for i, t in enumerate(textures):
+            mats[i].ka[:] = list(t.ka)
+            mats[i].kd[:] = list(t.kd)
+            mats[i].ks[:] = list(t.ks)
+            mats[i].alpha = t.alpha
+            mats[i].map_ka = t.map_ka.id if t.map_ka is not None else -1
+            mats[i].map_kd = t.map_kd.id if t.map_kd is not None else -1
+        out = ctypes.c_int32()
+        _chk(self.ctx.lib.dg_object_create(self.ctx.h, _ptr(v), v.shape[0], _ptr(n), n.shape[0], _ptr(uv),
+                                           uv.shape[0], ctypes.cast(md, ctypes.c_void_p), len(meshes),
+                                           ctypes.cast(mats, ctypes.c_void_p), len(textures), ctypes.byref(out)),
+             "Object::new")
+        self.id = out.value
+        self.meshes = meshes
+        self.textures = textures
+
+    def mesh_info_list(self) -> list:  # object.rs:456-476 (opaque meshes first, then transparent)
+        op = [m for m in self.meshes if self.textures[m.texture_idx].alpha >= 1.0 or
+              np.isnan(self.textures[m.texture_idx].alpha)]
+        tr = [m for m in self.meshes if m not in op]
+        return [MeshInfo(m.name, int(np.asarray(m.triangles).reshape(-1, 9).shape[0]),
+                         self.textures[m.texture_idx].name) for m in op + tr]
+
+
+class Camera:
+    """Scene.camera (scene/mod.rs:282-594): movement methods act on the scene's camera."""
+
+    def __init__(self, scene: "Scene"):
+        self._s = scene
+
+    def _op(self, op: int, *args):
+        a = np.zeros(3, np.float32)
+        a[: len(args)] = args
+        _chk(self._s.ctx.lib.dg_scene_camera_op(self._s.ctx.h, self._s.id, op, _ptr(a)), "camera")
+
+    def move_up(self, d): self._op(0, d)
+    def move_down(self, d): self._op(1, d)
+    def move_left(self, d): self._op(2, d)
+    def move_right(self, d): self._op(3, d)
+    def move_foward(self, d): self._op(4, d)  # noqa: E704 (reference spelling)
+    def move_backward(self, d): self._op(5, d)
+    def rotate_origin(self, theta_deg): self._op(6, theta_deg)
+    def set_pos(self, pos): self._op(7, *pos)
+
+    def get_pos(self) -> np.ndarray:
+        return self._get()[0]
+
+    def get_direction(self) -> np.ndarray:
+        return self._get()[1]
+
+    def _get(self):
+        p = np.zeros(3, np.float32)
+        d = np.zeros(3, np.float32)
+        _chk(self._s.ctx.lib.dg_scene_get_camera(self._s.ctx.h, self._s.id, _ptr(p), _ptr(d)), "camera")
+        return p, d
+
+    def reset(self, pos, direction, ratio, near=-10.0, far=-510.0, fov_x=135.0):
+        """Camera::new(pos, dir, ratio) with explicit projection constants."""
+        p = np.asarray(pos, np.float32)
+        d = np.asarray(direction, np.float32)
+        _chk(self._s.ctx.lib.dg_scene_set_camera(self._s.ctx.h, self._s.id, _ptr(p), _ptr(d), ratio, near, far,
+                                                 fov_x), "Camera::new")
+
+
+class Scene:
+    """Scene::new(width, height) (scene/mod.rs:760-786) and Scene::render."""
+
+    def __init__(self, width: int, height: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        out = ctypes.c_int32()
+        _chk(self.ctx.lib.dg_scene_create(self.ctx.h, width, height, ctypes.byref(out)), "Scene::new")
+        self.id = out.value
+        self.width, self.height = width, height
+        self.camera = Camera(self)
+        self._next_object_id = 0
+
+    def add_obj(self, obj: Object) -> ObjectInfo:
+        oid = ctypes.c_uint32()
+        _chk(self.ctx.lib.dg_scene_add_obj(self.ctx.h, self.id, obj.id, ctypes.byref(oid)), "Scene::add_obj")
+        return ObjectInfo(oid.value, obj.name, obj.mesh_info_list())
+
+    def move_camera_direction(self, dx: int, dy: int):
+        self.camera._op(8, dx, dy)
+
+    def set_lights(self, lights):
+        l = np.ascontiguousarray(lights, np.float32).reshape(-1, 3)
+        _chk(self.ctx.lib.dg_scene_set_lights(self.ctx.h, self.id, _ptr(l), l.shape[0]), "set_lights")
+
+    def set_exponent(self, e: int):
+        _chk(self.ctx.lib.dg_scene_set_exponent(self.ctx.h, self.id, int(e)), "set_exponent")
+
+    def frame_setup(self):
+        M = np.zeros(16, np.float32)
+        P = np.zeros(24, np.float32)
+        _chk(self.ctx.lib.dg_scene_frame_setup(self.ctx.h, self.id, _ptr(M), _ptr(P)), "frame_setup")
+        return M.reshape(4, 4), P.reshape(6, 4)
+
+    def render(self, canvas: "Canvas"):
+        _chk(self.ctx.lib.dg_scene_render(self.ctx.h, self.id, canvas.id), "Scene::render")
+
+
+class Canvas:
+    """Canvas (canvas.rs:353-983): BGRA colour buffer (row 0 = top) and f32 depth."""
+
+    def __init__(self, width: int, height: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        out = ctypes.c_int32()
+        _chk(self.ctx.lib.dg_canvas_create(self.ctx.h, width, height, ctypes.byref(out)), "Canvas::new")
+        self.id = out.value
+        self.width, self.height = width, height
+
+    def init_depth(self, depth: float):
+        _chk(self.ctx.lib.dg_canvas_init_depth(self.ctx.h, self.id, depth), "init_depth")
+
+    def apply_offset(self, x: int, y: int):
+        _chk(self.ctx.lib.dg_canvas_apply_offset(self.ctx.h, self.id, x, y), "apply_offset")
+
+    def resize(self, width: int, height: int):
+        _chk(self.ctx.lib.dg_canvas_resize(self.ctx.h, self.id, width, height), "resize")
+        self.width, self.height = width, height
+
+    def clear(self):
+        _chk(self.ctx.lib.dg_canvas_clear(self.ctx.h, self.id), "clear")
+
+    @staticmethod
+    def pixel_bytes() -> int:
+        return 4
+
+    def size_bytes(self) -> int:
+        return 4 * self.width * self.height
+
+    def as_bytes_slice(self) -> bytes:
+        return self.read()[0].tobytes()
+
+    def read(self, depth: bool = True):
+        """(bgra (H, W, 4) uint8 with row 0 = top, depth (H, W) float32 with row 0 = y 0)."""
+        bgra = np.empty((self.height, self.width, 4), np.uint8)
+        d = np.empty((self.height, self.width), np.float32) if depth else None
+        _chk(self.ctx.lib.dg_canvas_read(self.ctx.h, self.id, _ptr(bgra), _ptr(d)), "Canvas::read")
+        return bgra, d
+
+    def read_into(self, bgra: np.ndarray, depth: np.ndarray | None):
+        _chk(self.ctx.lib.dg_canvas_read(self.ctx.h, self.id, _ptr(bgra), _ptr(depth)), "Canvas::read")
+
+    def write(self, bgra: np.ndarray | None, depth: np.ndarray | None):
+        b = None if bgra is None else np.ascontiguousarray(bgra, np.uint8)
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+        _chk(self.ctx.lib.dg_canvas_write(self.ctx.h, self.id, _ptr(b), _ptr(d)), "Canvas::write")
+
+
+# ------------------------------------------------------------ scene builder
+@dataclass
+class BuiltScene:
+    scene: Scene
+    canvas: Canvas
+    objects: list
+    texmaps: list
+
+
+def build_scene(desc, ctx: Context | None = None) -> BuiltScene:
+    """Uploads a draw_gb300.scenes.SceneDesc: texture maps, objects, scene, camera, canvas."""
+    ctx = ctx or default_context()
+    texmaps = [TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in desc.textures]
+    scene = Scene(desc.width, desc.height, ctx)
+    scene.camera.reset(desc.cam_pos, desc.cam_dir, float(desc.ratio), desc.near, desc.far, desc.fov_x)
+    scene.set_lights(desc.lights)
+    scene.set_exponent(desc.exponent)
+    objects = []
+    for o in desc.objects:
+        mats = [Texture(f"m{i}", m.ka, m.kd, m.ks, m.alpha, texmaps[m.map_ka] if m.map_ka >= 0 else None,
+                        texmaps[m.map_kd] if m.map_kd >= 0 else None) for i, m in enumerate(o.materials)]
+        meshes = [IndexedMesh(f"mesh{i}", m.tris, m.texture_idx) for i, m in enumerate(o.meshes)]
+        ob = Object("object", o.vertices, o.normals, o.uvs, meshes, mats, ctx)
+        scene.add_obj(ob)
+        objects.append(ob)
+    cw, ch = desc.canvas_size
+    canvas = Canvas(cw, ch, ctx)
+    canvas.init_depth(desc.clear_depth)
+    canvas.apply_offset(*desc.offset)
+    return BuiltScene(scene, canvas, objects, texmaps)

@@ -1,0 +1,157 @@
+/*
+ * draw_gpu.h -- C ABI of the GB300 (sm_103a) rasterizer that replaces the CPU
+ * draw call of the reference renderer (mororo18/draw, Rust).
+ *
+ * The reference's boundary is `Scene::render(&mut self, canvas: &mut Canvas)`
+ * (src/renderer/scene/mod.rs:901) with its supporting object model. Each entry
+ * point below names the reference item it replaces. All functions return a
+ * dg_status (0 = DG_OK) and never abort; conditions on which the reference
+ * panics (assert!, unwrap, slice index) come back as error codes.
+ *
+ * Threading: one dg_ctx may be used by one host thread at a time
+ * (thread-compatible, like the reference's &mut Scene / &mut Canvas).
+ * Resources (texture maps, objects, scenes, canvases) are int32 ids owned by
+ * their context. Device work is enqueued on the context's CUDA stream; calls
+ * that hand data back to the host synchronize that stream.
+ *
+ * Colour buffers keep the reference's memory layout: BGRA bytes (Pixel,
+ * canvas.rs:51-59), row 0 = top of the screen (canvas.rs:941-942). Depth is
+ * f32 indexed y*W+x with y = 0 at the bottom (canvas.rs:413-423).
+ */
+#ifndef DRAW_GPU_H
+#define DRAW_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t dg_status;
+#define DG_OK 0
+#define DG_E_INVALID 1        /* bad argument; the reference panics (assert!/unwrap) */
+#define DG_E_INDEX 2          /* mesh index out of range (scene/mesh.rs:46-48 assert) */
+#define DG_E_TEXTURE_RANGE 3  /* texel offset outside the image (scene/mod.rs:151,167 slice index) */
+#define DG_E_CAMERA 4         /* camera / view-plane assertion (scene/mod.rs:327-331, 420, 624) */
+#define DG_E_DEPTH_UNINIT 5   /* render before init_depth (canvas.rs:914 debug_assert) */
+#define DG_E_CUDA 6           /* CUDA runtime error */
+#define DG_E_OOM 7            /* device memory exhausted or over budget */
+#define DG_E_LIMIT 8          /* size beyond a documented limit */
+#define DG_E_TIMEOUT 9        /* a bounded wait gave up */
+
+#define DG_MAX_LIGHTS 8
+
+typedef struct dg_ctx dg_ctx;
+
+/* Material: the reference's `Texture` (scene/mod.rs:206-216). map_ka/map_kd are
+ * texture-map ids from dg_texmap_create, or -1 for the 1x1 white default map
+ * (TextureMap::default, scene/mod.rs:128-135). */
+typedef struct {
+    float ka[3];
+    float kd[3];
+    float ks[3];
+    float alpha;
+    int32_t map_ka;
+    int32_t map_kd;
+} dg_material;
+
+/* One IndexedMesh (scene/mesh.rs:30-35): ntri triangles of 9 indices each in the
+ * reference's tuple order (position[3], texture[3], normal[3]; object.rs:431-434),
+ * drawn with material texture_idx of its object. */
+typedef struct {
+    const uint32_t* tris;
+    uint64_t ntri;
+    int32_t texture_idx;
+} dg_mesh_desc;
+
+/* ------------------------------------------------------------------ context */
+/* device >= 0: a CUDA device. device == -1: a host-only context in which scenes,
+ * cameras and dg_scene_frame_setup work and every device call returns DG_E_CUDA. */
+dg_status dg_ctx_create(int32_t device, dg_ctx** out);
+dg_status dg_ctx_destroy(dg_ctx* ctx);
+const char* dg_status_string(dg_status s);
+/* Waits for the context stream and returns (and clears) any error the kernels raised. */
+dg_status dg_ctx_synchronize(dg_ctx* ctx);
+/* Replaces the context's stream (cudaStream_t passed as void*; NULL = own stream). */
+dg_status dg_ctx_set_stream(dg_ctx* ctx, void* stream);
+void* dg_ctx_stream(dg_ctx* ctx);
+/* Per-kernel CUDA-event timing of the last render (ms); names: "vertex", "setup_raster",
+ * "large_raster", "resolve". Enabled with dg_ctx_set_timing(ctx, 1). */
+dg_status dg_ctx_set_timing(dg_ctx* ctx, int32_t enable);
+dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
+/* Counters of the last render: [0] vertices, [1] input triangles, [2] large triangles,
+ * [3] large 8x8 blocks, [4] covered pixels (written by resolve). Synchronizes. */
+dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
+
+/* -------------------------------------------------------------- texture map */
+/* TextureMap::new(img, width, height, components), scene/mod.rs:113-126. */
+dg_status dg_texmap_create(dg_ctx* ctx, const uint8_t* img, uint64_t len, uint64_t width, uint64_t height,
+                           uint64_t components, int32_t* out_id);
+
+/* ------------------------------------------------------------------- object */
+/* Object::new(name, vertices, normals, texture_vertices, meshes, textures),
+ * object.rs:34-71. vertices/normals/uvs are Vec3 lists (3 floats each; the
+ * reference stores UVs as Vec3 with z = 0, object.rs:151-155). Meshes whose
+ * material alpha < 1 form the transparent pass (object.rs:45-53). Indices are
+ * validated here (the reference asserts them during render). */
+dg_status dg_object_create(dg_ctx* ctx, const float* vertices, uint64_t nv, const float* normals, uint64_t nn,
+                           const float* uvs, uint64_t nuv, const dg_mesh_desc* meshes, uint64_t nmesh,
+                           const dg_material* materials, uint64_t nmat, int32_t* out_id);
+dg_status dg_object_destroy(dg_ctx* ctx, int32_t object);
+
+/* -------------------------------------------------------------------- scene */
+/* Scene::new(width, height), scene/mod.rs:760-786: camera at (0,0,150) looking
+ * at the origin, light at (0,300,300). */
+dg_status dg_scene_create(dg_ctx* ctx, uint64_t width, uint64_t height, int32_t* out_id);
+/* Scene::add_obj(obj) -> ObjectInfo.id, scene/mod.rs:788-801. */
+dg_status dg_scene_add_obj(dg_ctx* ctx, int32_t scene, int32_t object, uint32_t* out_obj_id);
+/* Camera::new(pos, dir, ratio), scene/mod.rs:297-357, with the projection
+ * constants explicit (reference: near=-10, far=-510, fov_x=135 degrees). */
+dg_status dg_scene_set_camera(dg_ctx* ctx, int32_t scene, const float pos[3], const float dir[3], float ratio,
+                              float near_, float far_, float fov_x_deg);
+/* Camera movement: op 0 move_up, 1 move_down, 2 move_left, 3 move_right,
+ * 4 move_foward, 5 move_backward (arg[0] = dist; scene/mod.rs:381-405),
+ * 6 rotate_origin(arg[0] degrees; :407-413), 7 set_pos(arg[0..3]; :377-379),
+ * 8 Scene::move_camera_direction(dx = arg[0], dy = arg[1]; :803-813). */
+dg_status dg_scene_camera_op(dg_ctx* ctx, int32_t scene, int32_t op, const float* arg);
+dg_status dg_scene_get_camera(dg_ctx* ctx, int32_t scene, float pos[3], float dir[3]);
+/* Extensions (reference: one light at Scene.light_source, exponent 2 at canvas.rs:724). */
+dg_status dg_scene_set_lights(dg_ctx* ctx, int32_t scene, const float* pos, uint32_t n);
+dg_status dg_scene_set_exponent(dg_ctx* ctx, int32_t scene, int32_t exponent);
+/* Host frame setup of Scene::render (gen_transformation_matrix, scene/mod.rs:817-899,
+ * and Camera::gen_view_planes, :481-593): M row-major, planes near, far, right,
+ * left, top, bottom as (normal xyz, k). Updates the camera basis like render. */
+dg_status dg_scene_frame_setup(dg_ctx* ctx, int32_t scene, float M[16], float planes[24]);
+/* Reads the current order of a transparent mesh's triangles (the reference
+ * re-sorts them in place every frame, scene/mod.rs:1100-1115). */
+dg_status dg_object_transparent_tris(dg_ctx* ctx, int32_t object, uint32_t mesh, uint32_t* out, uint64_t cap,
+                                     uint64_t* out_ntri);
+
+/* ------------------------------------------------------------------- canvas */
+/* Canvas::new(width, height), canvas.rs:366-380 (frame black, depth absent). */
+dg_status dg_canvas_create(dg_ctx* ctx, uint64_t width, uint64_t height, int32_t* out_id);
+dg_status dg_canvas_destroy(dg_ctx* ctx, int32_t canvas);
+dg_status dg_canvas_init_depth(dg_ctx* ctx, int32_t canvas, float depth);          /* canvas.rs:403-411 */
+dg_status dg_canvas_apply_offset(dg_ctx* ctx, int32_t canvas, int32_t x, int32_t y); /* canvas.rs:382-385 */
+dg_status dg_canvas_resize(dg_ctx* ctx, int32_t canvas, uint64_t width, uint64_t height); /* canvas.rs:387-393 */
+dg_status dg_canvas_clear(dg_ctx* ctx, int32_t canvas);                            /* canvas.rs:425-433 */
+/* Canvas::as_bytes_slice (canvas.rs:974-978) and the depth buffer, copied to host
+ * memory (either pointer may be NULL). Synchronizes; returns kernel errors. */
+dg_status dg_canvas_read(dg_ctx* ctx, int32_t canvas, uint8_t* bgra, float* depth);
+dg_status dg_canvas_write(dg_ctx* ctx, int32_t canvas, const uint8_t* bgra, const float* depth);
+/* Device pointers of the canvas buffers (for zero-copy consumers). */
+dg_status dg_canvas_device_ptrs(dg_ctx* ctx, int32_t canvas, void** bgra, void** depth);
+dg_status dg_canvas_size(dg_ctx* ctx, int32_t canvas, uint64_t* width, uint64_t* height);
+
+/* ------------------------------------------------------------------- render */
+/* Scene::render(&mut canvas), scene/mod.rs:901-1249: enqueued on the context
+ * stream; results are bit-identical to the reference's serial loop. */
+dg_status dg_scene_render(dg_ctx* ctx, int32_t scene, int32_t canvas);
+/* Renders n independent (scene, canvas) frames with one launch per pipeline
+ * stage (the batched form). Equivalent to n dg_scene_render calls. */
+dg_status dg_render_batch(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
