@@ -1,0 +1,479 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 rasterizer against the reference renderer's CPU path.
+
+One step = one call of the draw path (Scene::render) over one frame of the
+headline workload: a seeded 1920x1080 scene of 500 UV spheres x 2,000
+triangles (1M triangles, flattened into one object), a 2048^2 RGBA8 texture and
+2 point lights, rendered bit-exactly to the reference semantics. Meshes and
+textures are resident in HBM (uploaded once, like Scene::add_obj).
+
+  value     frames/s, device time of K steps measured with CUDA events on the
+            library's stream; L2 is flushed (256 MiB write) before every step
+  e2e       frames/s through the C ABI with host buffers: each step uploads the
+            frame descriptor (camera, lights, planes) and reads the BGRA frame
+            and the depth buffer back into pinned host memory
+  roofline  the dominant kernel's algorithmic bytes / its CUDA-event time,
+            against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
+  cpu_baseline  the CPU oracle (a C++ restatement of the reference renderer,
+            which is single-threaded Rust that cannot be built here) on all
+            host cores, independent frames, bounded sample
+  batched   the mixed-size batch workload (256 frames, 128^2..512^2, 1k..200k
+            triangles): the batched form (one launch per stage for all frames)
+            against the plain one-frame-per-launch path
+
+--impl reference runs only the CPU reference arm and prints its own line.
+Multi-GPU (torchrun): replicas only, one render context per rank, no collective
+on the data path; value = frames of all ranks / max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = ("plain pipeline at scale: 1920x1080, 1,000,000 triangles (500 seeded UV spheres x 2,000 tris, "
+            "radius U[0.2,1], centres uniform in a 20^3 box, camera at the box centre), 2048^2 RGBA8 texture, "
+            "2 point lights, exponent 2, depth cleared to +inf")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
+    ap.add_argument("--batch-frames", type=int, default=256)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def headline_scene():
+    from draw_gb300 import scenes
+
+    return scenes.sphere_field(width=1920, height=1080, n_spheres=500, slices=50, stacks=21, seed=1234, tex=2048,
+                               n_lights=2)
+
+
+def algorithmic_bytes(desc) -> dict:
+    """Per-frame algorithmic bytes of the draw path and their split by kernel.
+
+    Frame: V_pos*12 + V_nrm*12 + V_uv*8 + T*36 + texture bytes + W*H*8.
+    vertex reads the positions, setup_raster the position index triples,
+    resolve the uv/normal index triples, normals, uvs, texture maps and writes
+    colour + depth; queue_raster moves only intermediate data."""
+    V = sum(o.vertices.shape[0] for o in desc.objects)
+    N = sum(o.normals.shape[0] for o in desc.objects)
+    U = sum(o.uvs.shape[0] for o in desc.objects)
+    T = desc.n_tris
+    tex = sum(t.width * t.height * 4 for t in desc.textures)
+    W, H = desc.canvas_size
+    per = {
+        "vertex": V * 12,
+        "setup_raster": T * 12,
+        "queue_raster": 0,
+        "resolve": T * 24 + N * 12 + U * 8 + tex + W * H * 8,
+    }
+    per["frame"] = sum(per.values())
+    return per
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_uuid: str | None):
+        self.uuid = device_uuid
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"]
+        if self.uuid:
+            cmd += ["-i", self.uuid]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+            return
+        t0 = time.time()  # wait for the first sample so the timed region is covered
+        while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def mark(self):
+        """Index of the first sample taken inside the timed region."""
+        self.first = len(self.lines)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        lines = self.lines[getattr(self, "first", 0):] or self.lines[-1:]
+        for ln in lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, v: float) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------- CPU oracle leg
+class OracleFarm:
+    """The CPU oracle rendering independent frames of one scene on `threads`
+    host threads (one oracle context, i.e. one copy of the scene, per thread).
+    ctypes releases the GIL during each render call."""
+
+    def __init__(self, desc, threads: int):
+        import oracle
+
+        oracle.load()
+        self.desc = desc
+        self.threads = threads
+        self.ctxs = []
+        for _ in range(threads):
+            o = oracle.Oracle()
+            texs = [o.texmap(t.img, t.width, t.height, t.comps) for t in desc.textures]
+            s = o.scene(desc.width, desc.height)
+            o.set_camera(s, desc.cam_pos, desc.cam_dir, desc.ratio, desc.near, desc.far, desc.fov_x)
+            o.set_lights(s, desc.lights)
+            o.set_exponent(s, desc.exponent)
+            for ob in desc.objects:
+                mats = [dict(ka=m.ka, kd=m.kd, ks=m.ks, alpha=m.alpha,
+                             map_ka=texs[m.map_ka] if m.map_ka >= 0 else -1,
+                             map_kd=texs[m.map_kd] if m.map_kd >= 0 else -1) for m in ob.materials]
+                o.add_obj(s, o.object(ob.vertices, ob.normals, ob.uvs,
+                                      [(m.tris, m.texture_idx) for m in ob.meshes], mats))
+            cw, ch = desc.canvas_size
+            c = o.canvas(cw, ch)
+            o.init_depth(c, desc.clear_depth)
+            self.ctxs.append((o, s, c))
+
+    def single(self):
+        """One frame on one thread: (seconds, frame)."""
+        o, s, c = self.ctxs[0]
+        t = time.perf_counter()
+        o.render(s, c)
+        dt = time.perf_counter() - t
+        return dt, o.read(c, *self.desc.canvas_size)
+
+    def run(self, frames_per_thread: int) -> float:
+        """Every thread renders frames_per_thread frames; returns the wall time."""
+        def work(i):
+            o, s, c = self.ctxs[i]
+            for _ in range(frames_per_thread):
+                o.render(s, c)
+
+        th = [threading.Thread(target=work, args=(i,)) for i in range(self.threads)]
+        t = time.perf_counter()
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        return time.perf_counter() - t
+
+    def close(self):
+        for o, _, _ in self.ctxs:
+            o.close()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    desc = headline_scene()
+    threads = os.cpu_count() or 1
+    farm = OracleFarm(desc, threads)
+    t1, _ = farm.single()
+    # Each step renders one frame per host thread; the number of timed steps is
+    # capped so the whole arm stays within about two minutes of CPU time.
+    warm = min(args.warmup, 3)
+    step_s = max(t1, 1e-3)
+    steps = max(1, min(args.steps, int(90.0 / step_s)))
+    for _ in range(warm):
+        farm.run(1)
+    wall = sum(farm.run(1) for _ in range(steps))
+    farm.close()
+    value = steps * threads / wall
+    line = {
+        "impl": "reference", "metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * wall / steps, "steps_requested": args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"each step renders one frame per host thread ({threads} threads); "
+                                   f"single-thread frame time {t1 * 1000:.1f} ms"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is single-threaded Rust with no toolchain on this machine; this arm times the "
+                "C++ restatement of its render path (oracle/draw_oracle.cpp) on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------- GPU leg
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    from draw_gb300 import _build, renderer
+
+    if rank == 0 or not os.path.exists(_build.LIB):
+        _build.build()
+    barrier(world)
+    torch.cuda.set_device(local)
+    dev_uuid = None
+    try:
+        u = str(torch.cuda.get_device_properties(local).uuid)
+        dev_uuid = u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        pass
+    stream = torch.cuda.Stream()
+    ctx = renderer.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    desc = headline_scene()
+    built = renderer.build_scene(desc, ctx)
+    scene, canvas = built.scene, built.canvas
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    ab = algorithmic_bytes(desc)
+    peak, peak_kind = measured_peak()
+
+    clocks = ClockSampler(dev_uuid)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            scene.render(canvas)
+        torch.cuda.synchronize()
+        stats = ctx.last_stats()
+        ctx.set_timing(True)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kt = {k: [] for k in ["vertex", "setup_raster", "queue_raster", "resolve"]}
+        barrier(world)
+        torch.cuda.synchronize()
+        clocks.mark()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            scene.render(canvas)
+            ends[i].record(stream)
+            for k, v in ctx.kernel_times().items():
+                kt[k].append(v)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier(world)
+        clk = clocks.stop()
+        ctx.set_timing(False)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_ms = sum(step_ms)
+    dev_ms_max = allmax(world, dev_ms)
+    value = world * args.steps / (dev_ms_max / 1000.0)
+    kmean = {k: statistics.mean(v) for k, v in kt.items()}
+    dom = max(["vertex", "setup_raster", "resolve", "queue_raster"], key=lambda k: kmean[k])
+    frame_ms = sum(kmean.values())
+
+    # e2e: reference-facing call with host buffers
+    W, H = desc.canvas_size
+    pin_bgra = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    pin_depth = torch.empty((H, W), dtype=torch.float32, pin_memory=True).numpy()
+    pos = np.asarray(desc.cam_pos, np.float32)
+    for _ in range(args.warmup):
+        scene.camera.set_pos(pos)
+        scene.render(canvas)
+        canvas.read_into(pin_bgra, pin_depth)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        scene.camera.set_pos(pos)
+        scene.render(canvas)
+        canvas.read_into(pin_bgra, pin_depth)
+    e2e_s = allmax(world, time.perf_counter() - t0)
+    e2e = {"value": world * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": int(stats["h2d_bytes"]),
+           "d2h_bytes_per_step": int(W * H * 8)}
+
+    line = {
+        "metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded UV-sphere field)",
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+                   "l2": "flushed before every timed step (256 MiB write)", "resident_inputs": True},
+        "mtris_per_s": value * desc.n_tris / 1e6,
+        "mshaded_frags_per_s": value * stats["covered_pixels"] / 1e6,
+        "wall_ms_per_step": 1000.0 * wall / args.steps,
+        "kernels_ms": kmean,
+        "frame_stats": {k: int(v) for k, v in stats.items()},
+        "gpu_launches": int(stats["launches"]) * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ab[dom] / (kmean[dom] * 1e-3) / 1e9,
+                     "peak": peak, "unit": "GB/s", "frac": ab[dom] / (kmean[dom] * 1e-3) / 1e9 / peak,
+                     "traffic": read_traffic(dom), "peak_kind": peak_kind,
+                     "algorithmic_bytes": ab[dom]},
+        "frame_roofline": {"achieved": ab["frame"] / (frame_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                           "frac": ab["frame"] / (frame_ms * 1e-3) / 1e9 / peak,
+                           "algorithmic_bytes": ab["frame"], "kernel_ms_sum": frame_ms, "peak_kind": peak_kind},
+        "e2e": e2e,
+        "clocks": clk,
+    }
+
+    if rank == 0 and world == 1 and not args.no_batch:
+        line["batched"] = batched_leg(ctx, stream, args.batch_frames)
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        bgra, depth = canvas.read()
+        threads = os.cpu_count() or 1
+        farm = OracleFarm(desc, threads)
+        t1, first = farm.single()
+        per_thread = max(1, int(math.ceil(args.cpu_seconds / max(t1, 1e-3) / 2)))
+        cwall = farm.run(per_thread)
+        farm.close()
+        n = per_thread * threads
+        line["cpu_baseline"] = {"value": n / cwall, "unit": "frames/s", "cores": threads, "kind": "port",
+                                "sample": f"{n} frames of the headline scene on {threads} host threads "
+                                          f"({per_thread} per thread; single-thread frame {t1 * 1000:.1f} ms)"}
+        rd, gd = first.depth.view(np.uint32), depth.view(np.uint32)
+        diff = np.abs(first.bgra.astype(np.int16) - bgra.astype(np.int16))
+        line["parity"] = {"depth_bits_equal": bool(np.array_equal(rd, gd)),
+                          "coverage_equal": bool(np.array_equal(np.isfinite(first.depth), np.isfinite(depth))),
+                          "colour_max_lsb": int(diff.max()), "colour_frac_diff": float((diff.max(-1) > 0).mean())}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def batched_leg(ctx, stream, n_frames: int) -> dict:
+    """Mixed-size batch: the batched form vs one frame per launch sequence."""
+    import torch
+
+    from draw_gb300 import renderer, scenes
+
+    frames = scenes.batch_frames(n_frames=n_frames, seed=1234)
+    built = [renderer.build_scene(d, ctx) for d in frames]
+    sc = [b.scene for b in built]
+    cv = [b.canvas for b in built]
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            for s, c in zip(sc, cv):
+                s.render(c)
+            ctx.render_batch(sc, cv)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        reps = 3
+        e[0].record(stream)
+        for _ in range(reps):
+            for s, c in zip(sc, cv):
+                s.render(c)
+        e[1].record(stream)
+        e[2].record(stream)
+        for _ in range(reps):
+            ctx.render_batch(sc, cv)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+    plain_ms = e[0].elapsed_time(e[1]) / reps
+    batch_ms = e[2].elapsed_time(e[3]) / reps
+    tris = sum(d.n_tris for d in frames)
+    out = {"frames": n_frames, "triangles": tris, "pixels": sum(d.width * d.height for d in frames),
+           "plain_frames_per_s": n_frames / (plain_ms * 1e-3), "batched_frames_per_s": n_frames / (batch_ms * 1e-3),
+           "speedup": plain_ms / batch_ms, "batched_mtris_per_s": tris / (batch_ms * 1e-3) / 1e6,
+           "workload": "256 frames, side log-uniform 128..512, 1k..200k triangles (torus/sphere), "
+                       "textures 256^2..1024^2 from a pool of 32; L2 not flushed (working set > L2)"}
+    return out
+
+
+_TRAFFIC = None
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        with open(path) as f:
+            for ln in f:
+                parts = ln.split()
+                if len(parts) >= 2 and parts[0] == kernel and not ln.startswith("#"):
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -254,10 +254,13 @@ struct dg_ctx {
     size_t vrec_cap = 0;
     float4* d_vshade = nullptr;
     size_t vshade_cap = 0;
-    DgLargeRec* d_large = nullptr;
-    uint32_t* d_large_base = nullptr;
-    size_t large_cap = 0;
-    unsigned long long* d_counters = nullptr;  // [0] large counter, [1] covered px, [2] overflow
+    uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
+    size_t vmark_cap = 0;
+    DgQueueRec* d_queue = nullptr;
+    uint32_t* d_queue_base = nullptr;
+    size_t queue_cap = 0;
+    uint32_t small_max_px = DG_SMALL_MAX_PX;
+    unsigned long long* d_counters = nullptr;  // [0] queue counter, [1] covered px, [2] overflow
     uint32_t* d_err = nullptr;
     // job descriptors: pinned staging ring + device copies
     static const int kSlots = 4;
@@ -270,7 +273,7 @@ struct dg_ctx {
     bool timing = false;
     cudaEvent_t ev[5] = {};
     bool ev_valid = false;
-    uint64_t last_vtx = 0, last_tri = 0;
+    uint64_t last_vtx = 0, last_tri = 0, last_h2d = 0, last_launches = 0;
 };
 
 namespace {
@@ -470,17 +473,25 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
     if (e) return e;
     e = grow(c, &c->d_vshade, &c->vshade_cap, std::max<uint64_t>(total_vtx * stride * 2, 1));
     if (e) return e;
-    size_t want_large = std::max<size_t>(1u << 16, (size_t)(total_tri / 4));
-    if (c->large_cap < want_large) {
+    const size_t want_mark = std::max<uint64_t>((total_vtx + 31) / 32, 1);
+    if (c->vmark_cap < want_mark) {
+        e = grow(c, &c->d_vmark, &c->vmark_cap, want_mark);
+        if (e) return e;
+        DG_CUDA(cudaMemsetAsync(c->d_vmark, 0, c->vmark_cap * sizeof(uint32_t), c->stream));
+    }
+    // Queue capacity: every input triangle may produce up to 4 queued clip outputs; the
+    // cap keeps the scratch bounded (overflowing triangles are rasterized in place).
+    size_t want_queue = std::min<size_t>(std::max<size_t>(1u << 16, (size_t)total_tri), (1u << 24) - 1);
+    if (c->queue_cap < want_queue) {
         DG_CUDA(cudaStreamSynchronize(c->stream));
-        dfree(c->d_large);
-        dfree(c->d_large_base);
-        c->large_cap = 0;
-        e = dalloc(&c->d_large, want_large);
+        dfree(c->d_queue);
+        dfree(c->d_queue_base);
+        c->queue_cap = 0;
+        e = dalloc(&c->d_queue, want_queue);
         if (e) return e;
-        e = dalloc(&c->d_large_base, want_large);
+        e = dalloc(&c->d_queue_base, want_queue);
         if (e) return e;
-        c->large_cap = want_large;
+        c->queue_cap = want_queue;
     }
 
     // job descriptor upload through a pinned staging slot
@@ -517,15 +528,19 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
     job.shade_stride = stride;
     job.vrec = c->d_vrec;
     job.vshade = c->d_vshade;
-    job.large = c->d_large;
-    job.large_base = c->d_large_base;
-    job.large_cap = (uint32_t)std::min<size_t>(c->large_cap, (1u << 24) - 1);
-    job.large_counter = c->d_counters;
+    job.vmark = c->d_vmark;
+    job.queue = c->d_queue;
+    job.queue_base = c->d_queue_base;
+    job.queue_cap = (uint32_t)std::min<size_t>(c->queue_cap, (1u << 24) - 1);
+    job.small_max_px = c->small_max_px;
+    job.queue_counter = c->d_counters;
     job.stats = c->d_counters + 1;
     job.tex = c->d_tex;
     job.err = c->d_err;
     c->last_vtx = total_vtx;
     c->last_tri = total_tri;
+    c->last_h2d = need;
+    c->last_launches = (total_vtx ? 1 : 0) + (total_tri ? 2 : 0) + (total_tiles ? 1 : 0);
 
     DG_CUDA(cudaMemsetAsync(c->d_counters, 0, 3 * sizeof(unsigned long long), c->stream));
     if (c->timing) DG_CUDA(cudaEventRecord(c->ev[0], c->stream));
@@ -533,7 +548,7 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
     if (c->timing) DG_CUDA(cudaEventRecord(c->ev[1], c->stream));
     DG_CUDA(dg_launch_setup_raster(job, c->nsm, c->stream));
     if (c->timing) DG_CUDA(cudaEventRecord(c->ev[2], c->stream));
-    DG_CUDA(dg_launch_large_raster(job, c->nsm, c->stream));
+    DG_CUDA(dg_launch_queue_raster(job, c->nsm, c->stream));
     if (c->timing) DG_CUDA(cudaEventRecord(c->ev[3], c->stream));
     DG_CUDA(dg_launch_resolve(job, c->stream));
     if (c->timing) {
@@ -617,7 +632,7 @@ dg_status dg_ctx_destroy(dg_ctx* c) {
     for (auto& v : c->canvases) {
         dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
     }
-    dfree(c->d_tex); dfree(c->d_vrec); dfree(c->d_vshade); dfree(c->d_large); dfree(c->d_large_base);
+    dfree(c->d_tex); dfree(c->d_vrec); dfree(c->d_vshade); dfree(c->d_vmark); dfree(c->d_queue); dfree(c->d_queue_base);
     dfree(c->d_counters); dfree(c->d_err);
     for (int i = 0; i < dg_ctx::kSlots; i++) {
         if (c->h_stage[i]) cudaFreeHost(c->h_stage[i]);
@@ -671,8 +686,9 @@ dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
     DG_CUDA(cudaStreamSynchronize(c->stream));
     unsigned long long h[3];
     DG_CUDA(cudaMemcpy(h, c->d_counters, sizeof(h), cudaMemcpyDeviceToHost));
-    uint64_t v[6] = {c->last_vtx, c->last_tri, h[0] >> DG_PACK_SHIFT, h[0] & ((1ull << DG_PACK_SHIFT) - 1ull), h[1], h[2]};
-    for (int i = 0; i < n && i < 6; i++) out[i] = v[i];
+    uint64_t v[8] = {c->last_vtx, c->last_tri, h[0] >> DG_PACK_SHIFT, h[0] & ((1ull << DG_PACK_SHIFT) - 1ull),
+                     h[1], h[2], c->last_h2d, c->last_launches};
+    for (int i = 0; i < n && i < 8; i++) out[i] = v[i];
     return DG_OK;
 }
 

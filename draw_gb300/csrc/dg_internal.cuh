@@ -11,7 +11,7 @@
 //                   kept at DG_VIS_EMPTY between frames)
 //   render scratch: vrec float4[V_total] (snapped centre x,y, eye distance,
 //                   plane-sign masks), vshade float4[V_total*L*2] (light, halfway),
-//                   large-triangle records + their block bases, counters
+//                   raster-queue records + their work-unit bases, counters
 #pragma once
 
 #include <cstdint>
@@ -22,10 +22,12 @@
 #define DG_MAXL DG_MAX_LIGHTS
 #define DG_VIS_EMPTY 0xFFFFFFFFFFFFFFFFull
 
-// Triangles whose clipped bounding box has more pixels than this go to the
-// large-triangle pass (8x8 pixel blocks spread over all warps).
-#define DG_SMALL_MAX_PX 1024u
-#define DG_BLOCK 8u
+// Triangles whose clipped bounding box has at most this many pixels are
+// rasterized by the warp that set them up (default of DgJobDev.small_max_px);
+// larger ones go to the raster queue, whose pixels are spread over all warps
+// in units of DG_UNIT_PX row-major bounding-box pixels.
+#define DG_SMALL_MAX_PX 32u
+#define DG_UNIT_PX 32u
 // Resolve tile: 32 x 8 pixels, one CTA of 256 threads.
 #define DG_TILE_W 32u
 #define DG_TILE_H 8u
@@ -80,16 +82,16 @@ struct DgSegDev {
     const DgMatDev* mats;
 };
 
-// A triangle with too many bounding-box pixels for the warp-flattened path.
-struct DgLargeRec {
+// A triangle queued for the load-balanced raster pass (64 bytes).
+struct DgQueueRec {
     float ax, ay, bx, by, cx, cy;  // snapped centres
     float da, db, dc;              // vertex depths
     uint32_t seq;                  // frame-local key low word
     uint32_t frame;
-    uint32_t xlo, ylo, xhi, yhi;
-    uint32_t bw;       // blocks per row
-    uint32_t nblocks;
-    uint32_t pad[3];
+    uint32_t xlo, ylo;             // clipped bounding box origin
+    uint32_t w;                    // bounding box width in pixels
+    uint32_t npx;                  // bounding box pixels
+    uint32_t nunits;               // ceil(npx / DG_UNIT_PX), 0 if the record is rasterized elsewhere
 };
 
 struct DgJobDev {
@@ -100,12 +102,13 @@ struct DgJobDev {
     uint32_t shade_stride;  // lights per vertex row of vshade (max over frames)
     float4* vrec;
     float4* vshade;
-    DgLargeRec* large;
-    uint32_t* large_base;   // block base of each record (ascending)
-    uint32_t large_cap;
-    uint32_t pad0;
-    unsigned long long* large_counter;  // (records << 40) | blocks
-    unsigned long long* stats;          // [0] covered pixels, [1] overflowed large triangles
+    uint32_t* vmark;        // one bit per job vertex: needs light/halfway vectors (kept zero between jobs)
+    DgQueueRec* queue;
+    uint32_t* queue_base;   // first work unit of each record (ascending)
+    uint32_t queue_cap;
+    uint32_t small_max_px;  // in-warp raster threshold (bounding-box pixels)
+    unsigned long long* queue_counter;  // (records << 40) | work units
+    unsigned long long* stats;          // [0] covered pixels, [1] queued triangles rasterized in place
     const DgTexDev* tex;
     uint32_t* err;
 };
@@ -113,7 +116,7 @@ struct DgJobDev {
 // Host-side launchers (dg_kernels.cu).
 cudaError_t dg_launch_vertex(const DgJobDev& job, cudaStream_t s);
 cudaError_t dg_launch_setup_raster(const DgJobDev& job, int nsm, cudaStream_t s);
-cudaError_t dg_launch_large_raster(const DgJobDev& job, int nsm, cudaStream_t s);
+cudaError_t dg_launch_queue_raster(const DgJobDev& job, int nsm, cudaStream_t s);
 cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s);
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,
                            int fill_colour, int fill_depth, cudaStream_t s);

@@ -5,11 +5,12 @@
 //                   projected and snapped screen centre, plane-sign masks
 //                   (scene/mod.rs:917-926, :1047-1058, canvas.rs:585-587)
 //   k_setup_raster  per input triangle: back-face cull, lateral reject,
-//                   near/far clipping, bounding box, edge functions; small
+//                   near/far clipping, bounding box, edge functions; tiny
 //                   triangles are rasterized by their warp (pixels of all 32
-//                   lanes' boxes flattened with a warp prefix scan), large ones
+//                   lanes' boxes flattened with a warp prefix scan), the others
 //                   are queued (scene/mod.rs:933-1063, canvas.rs:585-681)
-//   k_large_raster  8x8 pixel blocks of the queued large triangles, one warp per block
+//   k_queue_raster  the queued triangles' bounding-box pixels in 32-pixel units
+//                   spread evenly over all warps
 //   k_resolve       per pixel: the winning fragment is shaded once
 //                   (canvas.rs:682-745, 906-930) and colour/depth are written
 //
@@ -193,8 +194,8 @@ __device__ __forceinline__ void raster_pixel(const EdgeSet& e, float da, float d
     float depth = interp(al, be, ga, da, db, dc);
     if (!(depth < fr.clear_depth)) return;
     uint64_t key = depth_key(depth, seq);
-    unsigned long long* p = reinterpret_cast<unsigned long long*>(fr.vis) + (uint64_t)y * fr.width + x;
-    if (key < __ldcg(p)) atomicMin(p, (unsigned long long)key);
+    // The result is unused, so this compiles to a fire-and-forget reduction at L2.
+    atomicMin(reinterpret_cast<unsigned long long*>(fr.vis) + (uint64_t)y * fr.width + x, (unsigned long long)key);
 }
 
 // Bounding box of the snapped centres, clipped to the screen exactly like
@@ -232,7 +233,9 @@ struct ClipProg {
     int nv, nout;
 };
 
-__device__ void build_clip(const DgFrameDev& fr, V3 a, V3 b, V3 c, ClipProg& P) {
+// Kept out of line: clipping is rare and would otherwise raise the register
+// allocation (and lower the occupancy) of the common path.
+__device__ __noinline__ void build_clip(const DgFrameDev& fr, V3 a, V3 b, V3 c, ClipProg& P) {
     P.pos[0] = a;
     P.pos[1] = b;
     P.pos[2] = c;
@@ -324,7 +327,8 @@ struct RTri {
 };
 
 // Screen centres and depths of clip output `o` (vertex ids < 3 reuse the vertex pass).
-__device__ void clip_output_tri(const DgFrameDev& fr, const ClipProg& P, int o, const float4 r[3], RTri& t) {
+__device__ __noinline__ void clip_output_tri(const DgFrameDev& fr, const ClipProg& P, int o, const float4 r[3],
+                                             RTri& t) {
     float cxs[3], cys[3];
     for (int i = 0; i < 3; i++) {
         int id = P.out[o][i];
@@ -347,6 +351,27 @@ __device__ __forceinline__ uint32_t seg_of_tri(const DgJobDev& job, uint32_t g) 
     return last_le(job.nsegs, g, [&](uint32_t i) { return job.segs[i].tri_begin; });
 }
 
+// Light and halfway vectors of job vertex v for every light (scene/mod.rs:920-925).
+// Only vertices of triangles that survive culling and clipping need them, so
+// they are computed after the setup pass for the vertices it marked.
+__device__ __forceinline__ void shade_vertex(const DgJobDev& job, uint32_t v) {
+    const uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
+    const DgSegDev& sg = job.segs[si];
+    const DgFrameDev& fr = job.frames[sg.frame];
+    const float4 p4 = __ldg(sg.pos + (v - sg.vtx_begin));
+    const V3 p = {p4.x, p4.y, p4.z};
+    const V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
+    const V3 eye = vnormalized(vsub(p, cam));
+    for (uint32_t l = 0; l < fr.nlights; l++) {
+        V3 L = {fr.light[l][0], fr.light[l][1], fr.light[l][2]};
+        V3 lt = vnormalized(vsub(p, L));
+        V3 h = vnormalized(vadd(lt, eye));
+        float4* dst = job.vshade + ((uint64_t)v * job.shade_stride + l) * 2;
+        dst[0] = make_float4(lt.x, lt.y, lt.z, h.x);
+        dst[1] = make_float4(h.y, h.z, 0.0f, 0.0f);
+    }
+}
+
 // ================================================================ kernels
 __global__ void __launch_bounds__(256) k_vertex(const DgJobDev job) {
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -357,17 +382,7 @@ __global__ void __launch_bounds__(256) k_vertex(const DgJobDev job) {
         float4 p4 = __ldg(sg.pos + (v - sg.vtx_begin));
         V3 p = {p4.x, p4.y, p4.z};
         V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
-        V3 eye_dir = vsub(p, cam);  // scene/mod.rs:920-925
-        V3 eye = vnormalized(eye_dir);
-        float depth = vnorm(eye_dir);
-        for (uint32_t l = 0; l < fr.nlights; l++) {
-            V3 L = {fr.light[l][0], fr.light[l][1], fr.light[l][2]};
-            V3 lt = vnormalized(vsub(p, L));
-            V3 h = vnormalized(vadd(lt, eye));
-            float4* dst = job.vshade + ((uint64_t)v * job.shade_stride + l) * 2;
-            dst[0] = make_float4(lt.x, lt.y, lt.z, h.x);
-            dst[1] = make_float4(h.y, h.z, 0.0f, 0.0f);
-        }
+        float depth = vnorm(vsub(p, cam));  // eye distance, scene/mod.rs:924
         float cx, cy;
         project_snap(fr, p, cx, cy);
         uint32_t mask = 0;
@@ -476,6 +491,10 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                     nout = P.nout;
                     clipped = true;
                 }
+                if (nout > 0) {  // its vertices need light/halfway vectors for shading
+                    const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
+                    for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+                }
             }
         }
         for (int rr = 0;; rr++) {
@@ -484,6 +503,8 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             RTri tr;
             EdgeSet e;
             uint32_t npx = 0;
+            uint32_t nu = 0;     // work units to queue (0: not queued)
+            uint64_t qpx = 0;    // bounding-box pixels of the queued triangle
             tr.xlo = tr.xhi = tr.ylo = tr.yhi = 0;
             tr.frame = 0;
             if (has) {
@@ -509,38 +530,59 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                     bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
                     make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
                     uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
-                    if (px <= DG_SMALL_MAX_PX) {
+                    if (px <= job.small_max_px) {
                         npx = (uint32_t)px;
                     } else {
-                        uint32_t bw = (tr.xhi - tr.xlo) / DG_BLOCK + 1u;
-                        uint32_t bh = (tr.yhi - tr.ylo) / DG_BLOCK + 1u;
-                        uint32_t nb = bw * bh;
-                        unsigned long long old =
-                            atomicAdd(job.large_counter, (1ull << DG_PACK_SHIFT) | (unsigned long long)nb);
-                        uint64_t rec = old >> DG_PACK_SHIFT;
-                        uint64_t bbase = old & ((1ull << DG_PACK_SHIFT) - 1ull);
-                        // A record whose blocks would pass 2^32 is stored with no blocks (base
-                        // saturated, so bases stay ascending) and rasterized by this lane.
-                        const bool fits = bbase + nb <= 0xFFFFFFFFull;
-                        if (rec < job.large_cap) {
-                            DgLargeRec L;
-                            L.ax = tr.ax; L.ay = tr.ay; L.bx = tr.bx; L.by = tr.by; L.cx = tr.cx; L.cy = tr.cy;
-                            L.da = tr.da; L.db = tr.db; L.dc = tr.dc;
-                            L.seq = tr.seq;
-                            L.frame = tr.frame;
-                            L.xlo = tr.xlo; L.ylo = tr.ylo; L.xhi = tr.xhi; L.yhi = tr.yhi;
-                            L.bw = bw;
-                            L.nblocks = fits ? nb : 0u;
-                            job.large[rec] = L;
-                            job.large_base[rec] = fits ? (uint32_t)bbase : 0xFFFFFFFFu;
-                        }
-                        if (!(rec < job.large_cap && fits)) {
-                            // queue full: this lane rasterizes the box itself
-                            atomicAdd(job.stats + 1, 1ull);
-                            for (uint32_t y = tr.ylo; y <= tr.yhi; y++)
-                                for (uint32_t x = tr.xlo; x <= tr.xhi; x++)
-                                    raster_pixel(e, tr.da, tr.db, tr.dc, tr.seq, x, y, fr);
-                        }
+                        qpx = px;
+                        nu = (uint32_t)((px + DG_UNIT_PX - 1u) / DG_UNIT_PX);
+                    }
+                }
+            }
+            // Queue this round's large triangles with one 64-bit atomic per warp: it hands out
+            // the record slots and their first work units together, so work-unit bases ascend
+            // with the slot (the queue pass binary-searches them).
+            const unsigned qmask = __ballot_sync(FULL, nu != 0u);
+            if (qmask) {
+                uint32_t incl = nu;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t v = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= (uint32_t)o) incl += v;
+                }
+                const uint32_t total_units = __shfl_sync(FULL, incl, 31);
+                const int leader = __ffs(qmask) - 1;
+                unsigned long long old = 0;
+                if ((int)lane == leader)
+                    old = atomicAdd(job.queue_counter,
+                                    ((unsigned long long)__popc(qmask) << DG_PACK_SHIFT) | total_units);
+                old = __shfl_sync(FULL, old, leader);
+                if (nu != 0u) {
+                    const uint64_t rec = (old >> DG_PACK_SHIFT) + __popc(qmask & ((1u << lane) - 1u));
+                    const uint64_t ubase = (old & ((1ull << DG_PACK_SHIFT) - 1ull)) + (incl - nu);
+                    // A record whose units would pass 2^32 is stored with no units (base
+                    // saturated, so bases stay ascending) and rasterized by this lane.
+                    const bool fits = ubase + nu <= 0xFFFFFFFFull;
+                    if (rec < job.queue_cap) {
+                        DgQueueRec q;
+                        q.ax = tr.ax; q.ay = tr.ay; q.bx = tr.bx; q.by = tr.by; q.cx = tr.cx; q.cy = tr.cy;
+                        q.da = tr.da; q.db = tr.db; q.dc = tr.dc;
+                        q.seq = tr.seq;
+                        q.frame = tr.frame;
+                        q.xlo = tr.xlo;
+                        q.ylo = tr.ylo;
+                        q.w = tr.xhi - tr.xlo + 1u;
+                        q.npx = (uint32_t)qpx;
+                        q.nunits = fits ? nu : 0u;
+                        job.queue[rec] = q;
+                        job.queue_base[rec] = fits ? (uint32_t)ubase : 0xFFFFFFFFu;
+                    }
+                    if (!(rec < job.queue_cap && fits)) {
+                        // queue full: this lane rasterizes the box itself
+                        atomicAdd(job.stats + 1, 1ull);
+                        const DgFrameDev& fr = job.frames[tr.frame];
+                        for (uint32_t y = tr.ylo; y <= tr.yhi; y++)
+                            for (uint32_t x = tr.xlo; x <= tr.xhi; x++)
+                                raster_pixel(e, tr.da, tr.db, tr.dc, tr.seq, x, y, fr);
                     }
                 }
             }
@@ -549,36 +591,55 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_large_raster(const DgJobDev job) {
+// The raster queue: the bounding-box pixels of every queued triangle, numbered
+// row-major in units of DG_UNIT_PX and spread over all warps. A warp keeps its
+// current record (and edge constants) while consecutive units belong to it.
+__global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const unsigned long long cnt = __ldcg(job.large_counter);
-    uint64_t nrec64 = cnt >> DG_PACK_SHIFT;
-    const uint32_t nrec = (uint32_t)(nrec64 < job.large_cap ? nrec64 : job.large_cap);
-    uint64_t nb64 = cnt & ((1ull << DG_PACK_SHIFT) - 1ull);
-    const uint32_t nblocks = (uint32_t)(nb64 < 0xFFFFFFFFull ? nb64 : 0xFFFFFFFFull);
+    // Prologue: light/halfway vectors of the vertices the setup pass marked, one
+    // mark word (32 vertices) per warp; the words are cleared for the next job.
+    const uint32_t nwords = (job.total_vtx + 31u) >> 5;
+    for (uint32_t w = warp; w < nwords; w += nwarps) {
+        const uint32_t bits = __ldcg(job.vmark + w);
+        if (bits == 0u) continue;
+        if (((bits >> lane) & 1u) && (w << 5) + lane < job.total_vtx) shade_vertex(job, (w << 5) + lane);
+        if (lane == 0) job.vmark[w] = 0u;
+    }
+    const unsigned long long cnt = __ldcg(job.queue_counter);
+    const uint64_t nrec64 = cnt >> DG_PACK_SHIFT;
+    const uint32_t nrec = (uint32_t)(nrec64 < job.queue_cap ? nrec64 : job.queue_cap);
+    const uint64_t nu64 = cnt & ((1ull << DG_PACK_SHIFT) - 1ull);
+    const uint32_t nunits = (uint32_t)(nu64 < 0xFFFFFFFFull ? nu64 : 0xFFFFFFFFull);
     if (nrec == 0) return;
     uint32_t cur_base = 1u, cur_end = 0u;
-    DgLargeRec L;
+    DgQueueRec q;
     EdgeSet e;
-    for (uint32_t b = warp; b < nblocks; b += nwarps) {
-        if (!(b >= cur_base && b < cur_end)) {
-            uint32_t ri = last_le(nrec, b, [&](uint32_t i) { return __ldg(job.large_base + i); });
-            L = job.large[ri];
-            cur_base = __ldg(job.large_base + ri);
-            cur_end = cur_base + L.nblocks;
-            if (!(b >= cur_base && b < cur_end)) continue;  // block of a record that did not fit the queue
-            make_edges(L.ax, L.ay, L.bx, L.by, L.cx, L.cy, e);
+    float rcp_w = 0.0f;
+    // Each warp takes a contiguous range of units, so consecutive units usually
+    // belong to the same record and the cached record and edge constants are reused.
+    const uint32_t per = (nunits + nwarps - 1u) / nwarps;
+    const uint32_t u0 = warp * per;
+    const uint32_t u1 = min(nunits, u0 + per);
+    for (uint32_t u = u0; u < u1; u++) {
+        if (!(u >= cur_base && u < cur_end)) {
+            uint32_t ri = last_le(nrec, u, [&](uint32_t i) { return __ldg(job.queue_base + i); });
+            q = job.queue[ri];
+            cur_base = __ldg(job.queue_base + ri);
+            cur_end = cur_base + q.nunits;
+            if (!(u >= cur_base && u < cur_end)) continue;  // unit of a record that did not fit the queue
+            make_edges(q.ax, q.ay, q.bx, q.by, q.cx, q.cy, e);
+            rcp_w = __frcp_rn((float)q.w);
         }
-        const DgFrameDev& fr = job.frames[L.frame];
-        uint32_t local = b - cur_base;
-        uint32_t by = local / L.bw, bx = local - by * L.bw;
-        uint32_t x0 = L.xlo + bx * DG_BLOCK, y0 = L.ylo + by * DG_BLOCK;
-#pragma unroll
-        for (uint32_t k = lane; k < DG_BLOCK * DG_BLOCK; k += 32u) {
-            uint32_t x = x0 + (k & (DG_BLOCK - 1u)), y = y0 + k / DG_BLOCK;
-            if (x <= L.xhi && y <= L.yhi) raster_pixel(e, L.da, L.db, L.dc, L.seq, x, y, fr);
+        const uint32_t k = (u - cur_base) * DG_UNIT_PX + lane;
+        if (k < q.npx) {
+            // k / w from a float reciprocal, corrected to the exact quotient
+            uint32_t yy = (uint32_t)__fmul_rz((float)k, rcp_w);
+            while ((uint64_t)yy * q.w > k) yy--;
+            while ((uint64_t)(yy + 1u) * q.w <= k) yy++;
+            const uint32_t xx = k - yy * q.w;
+            raster_pixel(e, q.da, q.db, q.dc, q.seq, q.xlo + xx, q.ylo + yy, job.frames[q.frame]);
         }
     }
 }
@@ -599,7 +660,7 @@ __device__ __forceinline__ bool tex_rgb(const DgTexDev& tx, float u, float v, ui
 
 // Shades the winning fragment of pixel (x, y): canvas.rs:682-741.
 __device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint32_t seq, uint32_t x, uint32_t y,
-                                float& depth_out, int& errc) {
+                                const float* inv255, float& depth_out, int& errc) {
     errc = DG_OK;
     const uint32_t tl = seq >> 2, o = seq & 3u;
     uint32_t si =
@@ -670,11 +731,10 @@ __device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint3
         errc = DG_E_TEXTURE_RANGE;
         return 0u;
     }
-    // Pixel::normalized_as_vec3 (canvas.rs:81-87)
-    const V3 diffuse = {fD((float)(kd_rgb & 0xFFu), 255.0f), fD((float)((kd_rgb >> 8) & 0xFFu), 255.0f),
-                        fD((float)((kd_rgb >> 16) & 0xFFu), 255.0f)};
-    const V3 ambient = {fD((float)(ka_rgb & 0xFFu), 255.0f), fD((float)((ka_rgb >> 8) & 0xFFu), 255.0f),
-                        fD((float)((ka_rgb >> 16) & 0xFFu), 255.0f)};
+    // Pixel::normalized_as_vec3 (canvas.rs:81-87): byte / 255.0, looked up in a
+    // table of the 256 correctly rounded quotients
+    const V3 diffuse = {inv255[kd_rgb & 0xFFu], inv255[(kd_rgb >> 8) & 0xFFu], inv255[(kd_rgb >> 16) & 0xFFu]};
+    const V3 ambient = {inv255[ka_rgb & 0xFFu], inv255[(ka_rgb >> 8) & 0xFFu], inv255[(ka_rgb >> 16) & 0xFFu]};
     const V3 c_l = {mat.ks[0], mat.ks[1], mat.ks[2]};
     const V3 c_r = {fM(diffuse.x, mat.kd[0]), fM(diffuse.y, mat.kd[1]), fM(diffuse.z, mat.kd[2])};
     const V3 c_a = {fM(ambient.x, mat.ka[0]), fM(ambient.y, mat.ka[1]), fM(ambient.z, mat.ka[2])};
@@ -705,6 +765,9 @@ __device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint3
 }
 
 __global__ void __launch_bounds__(256) k_resolve(const DgJobDev job) {
+    __shared__ float inv255[256];
+    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
+    __syncthreads();
     const uint32_t tile = blockIdx.x;
     const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
     const DgFrameDev& fr = job.frames[fi];
@@ -726,7 +789,7 @@ __global__ void __launch_bounds__(256) k_resolve(const DgJobDev job) {
             fr.vis[i] = DG_VIS_EMPTY;
             float d = 0.0f;
             int errc;
-            uint32_t c = shade_pixel(job, fr, (uint32_t)key, x, y, d, errc);
+            uint32_t c = shade_pixel(job, fr, (uint32_t)key, x, y, inv255, d, errc);
             if (errc != DG_OK) {
                 atomicOr(job.err, 1u << errc);
                 c = AZUL_BB;
@@ -771,9 +834,9 @@ cudaError_t dg_launch_setup_raster(const DgJobDev& job, int nsm, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t dg_launch_large_raster(const DgJobDev& job, int nsm, cudaStream_t s) {
+cudaError_t dg_launch_queue_raster(const DgJobDev& job, int nsm, cudaStream_t s) {
     if (job.total_tri == 0) return cudaSuccess;
-    k_large_raster<<<(unsigned)nsm * 8u, 256, 0, s>>>(job);
+    k_queue_raster<<<(unsigned)nsm * 8u, 256, 0, s>>>(job);
     return cudaGetLastError();
 }
 

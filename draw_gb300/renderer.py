@@ -140,12 +140,13 @@ class Context:
     def kernel_times(self) -> dict:
         ms = (ctypes.c_float * 4)()
         _chk(self.lib.dg_ctx_kernel_times(self.h, ms, 4), "kernel_times")
-        return dict(zip(["vertex", "setup_raster", "large_raster", "resolve"], list(ms)))
+        return dict(zip(["vertex", "setup_raster", "queue_raster", "resolve"], list(ms)))
 
     def last_stats(self) -> dict:
-        v = (ctypes.c_uint64 * 6)()
-        _chk(self.lib.dg_ctx_last_stats(self.h, v, 6), "last_stats")
-        keys = ["vertices", "triangles", "large_triangles", "large_blocks", "covered_pixels", "large_overflow"]
+        v = (ctypes.c_uint64 * 8)()
+        _chk(self.lib.dg_ctx_last_stats(self.h, v, 8), "last_stats")
+        keys = ["vertices", "triangles", "queued_triangles", "queued_units", "covered_pixels", "queue_overflow",
+                "h2d_bytes", "launches"]
         return dict(zip(keys, list(v)))
 
     def render_batch(self, scenes: list, canvases: list):

@@ -273,11 +273,11 @@ def mesh_for_tris(kind: str, n_tris: int, radius: float = 1.0):
 
 
 def random_frame(rng: np.random.Generator, width: int, height: int, n_tris: int, tex_side: int, seed: int,
-                 kind: str | None = None) -> SceneDesc:
+                 kind: str | None = None, texture: TextureDesc | None = None) -> SceneDesc:
     """One frame of a batch: its own mesh, camera and texture."""
     kind = kind or ("torus" if rng.random() < 0.5 else "sphere")
     pos, nrm, uv, tri = mesh_for_tris(kind, n_tris)
-    t = value_noise_checker(tex_side, tex_side, seed, comps=4)
+    t = texture if texture is not None else value_noise_checker(tex_side, tex_side, seed, comps=4)
     mat = Material((0.1,) * 3, (0.7,) * 3, (0.2,) * 3, 1.0, 0, 0)
     obj = ObjectDesc(pos, nrm, uv, [MeshDesc(_tris9(tri), 0)], [mat])
     az = rng.uniform(0, 2 * math.pi)
@@ -291,14 +291,19 @@ def random_frame(rng: np.random.Generator, width: int, height: int, n_tris: int,
 
 
 def batch_frames(n_frames=256, seed=1234, side_range=(128, 512), tri_range=(1_000, 200_000),
-                 tex_range=(256, 1024)) -> list:
-    """Batching workload: frames of side log-uniform in side_range, meshes of
-    log-uniform triangle count in tri_range, textures of side in tex_range."""
+                 tex_range=(256, 1024), tex_pool: int = 32) -> list:
+    """Batching workload: square frames of side log-uniform in side_range, meshes
+    of log-uniform triangle count in tri_range, textures of side in tex_range.
+    Textures come from a seeded pool of tex_pool maps (shared between frames)."""
     rng = np.random.Generator(np.random.PCG64(seed))
+    pool: dict = {}
     frames = []
     for i in range(n_frames):
         side = int(round(math.exp(rng.uniform(math.log(side_range[0]), math.log(side_range[1])))))
         ntri = int(round(math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))))
         tex = int(2 ** round(rng.uniform(math.log2(tex_range[0]), math.log2(tex_range[1]))))
-        frames.append(random_frame(rng, side, side, ntri, tex, seed + i))
+        key = (tex, i % tex_pool)
+        if key not in pool:
+            pool[key] = value_noise_checker(tex, tex, seed + key[1], comps=4)
+        frames.append(random_frame(rng, side, side, ntri, tex, seed + i, texture=pool[key]))
     return frames

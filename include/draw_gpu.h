@@ -76,11 +76,14 @@ dg_status dg_ctx_synchronize(dg_ctx* ctx);
 dg_status dg_ctx_set_stream(dg_ctx* ctx, void* stream);
 void* dg_ctx_stream(dg_ctx* ctx);
 /* Per-kernel CUDA-event timing of the last render (ms); names: "vertex", "setup_raster",
- * "large_raster", "resolve". Enabled with dg_ctx_set_timing(ctx, 1). */
+ * "queue_raster", "resolve". Enabled with dg_ctx_set_timing(ctx, 1). */
 dg_status dg_ctx_set_timing(dg_ctx* ctx, int32_t enable);
 dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
-/* Counters of the last render: [0] vertices, [1] input triangles, [2] large triangles,
- * [3] large 8x8 blocks, [4] covered pixels (written by resolve). Synchronizes. */
+/* Counters of the last render: [0] vertices, [1] input triangles, [2] triangles queued
+ * for the load-balanced raster pass, [3] their 32-pixel work units, [4] covered pixels
+ * (written by resolve), [5] queued triangles rasterized in place because the queue was
+ * full, [6] host-to-device bytes of the job descriptor, [7] kernels launched.
+ * Synchronizes. */
 dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
 
 /* -------------------------------------------------------------- texture map */
