@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
-SOURCES = ["dg_kernels.cu", "dg_api.cu"]
+SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_noalloc.cu"]
 HEADERS = ["dg_internal.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -560,6 +560,21 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
 
 }  // namespace
 
+// Camera::new followed by the per-frame host setup of Scene::render, for callers
+// that hold no dg_ctx; uses only stack storage.
+dg_status dg_host_frame_setup(uint64_t width, uint64_t height, const float pos[3], const float dir[3], float ratio,
+                              float near_, float far_, float fov_x_deg, float M[4][4], float planes[6][4]) {
+    if (width == 0 || height == 0 || !pos || !dir) return DG_E_INVALID;
+    Scene s;
+    s.width = width;
+    s.height = height;
+    s.exponent = 2;
+    dg_status e = camera_init(s.cam, h3(pos[0], pos[1], pos[2]), h3(dir[0], dir[1], dir[2]), ratio, near_, far_,
+                              fov_x_deg);
+    if (e) return e;
+    return frame_setup(s, M, planes);
+}
+
 extern "C" {
 
 const char* dg_status_string(dg_status s) {

@@ -121,3 +121,7 @@ cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s);
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,
                            int fill_colour, int fill_depth, cudaStream_t s);
 cudaError_t dg_launch_vis_reset(uint64_t* vis, uint64_t n, cudaStream_t s);
+
+// Host frame setup without a context (dg_api.cu).
+dg_status dg_host_frame_setup(uint64_t width, uint64_t height, const float pos[3], const float dir[3], float ratio,
+                              float near_, float far_, float fov_x_deg, float M[4][4], float planes[6][4]);

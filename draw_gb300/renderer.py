@@ -62,6 +62,7 @@ SIGNATURES = {
     "dg_canvas_size": (_i32, [_P, _i32, _P, _P]),
     "dg_scene_render": (_i32, [_P, _i32, _i32]),
     "dg_render_batch": (_i32, [_P, _P, _P, _u32]),
+    "dg_render_noalloc": (_i32, [_P, _P, _P, _u32, _P, _u32, _P, _P, _P, _P]),
 }
 
 
@@ -78,6 +79,30 @@ class dg_material(ctypes.Structure):
 
 class dg_mesh_desc(ctypes.Structure):
     _fields_ = [("tris", ctypes.c_void_p), ("ntri", ctypes.c_uint64), ("texture_idx", ctypes.c_int32)]
+
+
+# dg_render_noalloc's argument structs (include/draw_gpu.h).
+NOALLOC_MAX_LIGHTS = 2
+
+
+class dg_device_mesh(ctypes.Structure):
+    _fields_ = [("pos", ctypes.c_void_p), ("nrm", ctypes.c_void_p), ("uv", ctypes.c_void_p),
+                ("tri_pos", ctypes.c_void_p), ("tri_uv", ctypes.c_void_p), ("tri_nrm", ctypes.c_void_p),
+                ("nv", ctypes.c_uint32), ("nn", ctypes.c_uint32), ("nuv", ctypes.c_uint32), ("ntri", ctypes.c_uint32)]
+
+
+class dg_device_texmap(ctypes.Structure):
+    _fields_ = [("bytes", ctypes.c_void_p), ("len", ctypes.c_uint64), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("components", ctypes.c_uint32)]
+
+
+class dg_frame_params(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("canvas_width", ctypes.c_uint32),
+                ("canvas_height", ctypes.c_uint32), ("cam_pos", ctypes.c_float * 3), ("cam_dir", ctypes.c_float * 3),
+                ("near_", ctypes.c_float), ("far_", ctypes.c_float), ("fov_x_deg", ctypes.c_float),
+                ("lights", (ctypes.c_float * 3) * NOALLOC_MAX_LIGHTS), ("nlights", ctypes.c_uint32),
+                ("exponent", ctypes.c_int32), ("clear_depth", ctypes.c_float), ("offset_x", ctypes.c_int32),
+                ("offset_y", ctypes.c_int32)]
 
 
 _lib = None

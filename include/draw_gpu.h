@@ -154,6 +154,86 @@ dg_status dg_scene_render(dg_ctx* ctx, int32_t scene, int32_t canvas);
  * stage (the batched form). Equivalent to n dg_scene_render calls. */
 dg_status dg_render_batch(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n);
 
+/* ----------------------------------------------------- render without allocating
+ * No counterpart in the reference: an extra entry point for callers that cannot
+ * allocate device memory while they draw, for example a host application or
+ * plugin that owns a fixed device-memory budget and hands the renderer only its
+ * buffers, or a frame loop that must not stall on cudaMalloc/cudaFree (which
+ * synchronize the device). It renders one frame of one mesh like
+ * dg_scene_render, but all of its scratch memory (vertex records, the
+ * visibility buffer, the raster queue, counters, the job descriptor) lives in
+ * one statically sized __device__ array of the library (about 5.6 MiB, sized by
+ * the limits below), which every GPU that loads the library keeps until the
+ * process exits. It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * The caller passes its inputs and outputs as device pointers. Limits (checked,
+ * DG_E_LIMIT beyond them): DG_NOALLOC_MAX_VERTICES position vertices,
+ * DG_NOALLOC_MAX_TRIANGLES triangles, DG_NOALLOC_MAX_PIXELS canvas pixels,
+ * DG_NOALLOC_MAX_LIGHTS lights, DG_NOALLOC_MAX_TEXMAPS texture maps,
+ * DG_NOALLOC_MAX_MATERIALS materials. Precondition: every index is in range
+ * (what dg_object_create validates for the allocating path); the indices stay
+ * in device memory and are not read back.
+ *
+ * The work runs on the calling thread's current device, on `stream` (NULL = the
+ * default stream). The first call on a device looks up the scratch array's
+ * device address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the one scratch array, which keeps the last call's
+ * contents (each call re-initializes what must start empty): calls whose GPU
+ * work overlaps, on different streams or host threads, race and must not be
+ * issued. If status_out is not NULL the call waits for its work and stores the
+ * device-side status there (DG_OK or DG_E_TEXTURE_RANGE). */
+#define DG_NOALLOC_MAX_VERTICES 32768u
+#define DG_NOALLOC_MAX_TRIANGLES 65536u
+#define DG_NOALLOC_MAX_PIXELS 262144u
+#define DG_NOALLOC_MAX_LIGHTS 2u
+#define DG_NOALLOC_MAX_TEXMAPS 8u
+#define DG_NOALLOC_MAX_MATERIALS 16u
+
+/* A mesh resident in device memory, in the layout the kernels read:
+ * pos float4[nv] (x, y, z, 1), nrm float4[nn] (x, y, z, 0), uv float2[nuv],
+ * tri_pos uint4[ntri] (position indices a, b, c, material index),
+ * tri_uv uint4[ntri] and tri_nrm uint4[ntri] (index triples, 4th word unused). */
+typedef struct {
+    const void* pos;
+    const void* nrm;
+    const void* uv;
+    const void* tri_pos;
+    const void* tri_uv;
+    const void* tri_nrm;
+    uint32_t nv, nn, nuv, ntri;
+} dg_device_mesh;
+
+/* A texture map in device memory: `len` image bytes (TextureMap layout, row 0 =
+ * top), 4-byte aligned and readable up to the next multiple of 4 bytes plus 4. */
+typedef struct {
+    const void* bytes;
+    uint64_t len;
+    uint32_t width, height, components;
+} dg_device_texmap;
+
+/* Frame parameters: scene size (projection), canvas size, camera
+ * (Camera::new(pos, dir, width/height) with explicit near/far/fov_x), lights,
+ * specular exponent, depth clear value (Canvas::init_depth) and canvas offset. */
+typedef struct {
+    uint32_t width, height;
+    uint32_t canvas_width, canvas_height;
+    float cam_pos[3];
+    float cam_dir[3];
+    float near_, far_, fov_x_deg;
+    float lights[DG_NOALLOC_MAX_LIGHTS][3];
+    uint32_t nlights;
+    int32_t exponent;
+    float clear_depth;
+    int32_t offset_x, offset_y;
+} dg_frame_params;
+
+/* Renders `mesh` with `materials` (map ids index `texmaps`, -1 = 1x1 white) into
+ * bgra_out (u32[canvas pixels], Canvas byte layout) and depth_out
+ * (f32[canvas pixels]), both device pointers. */
+dg_status dg_render_noalloc(const dg_frame_params* params, const dg_device_mesh* mesh, const dg_material* materials,
+                            uint32_t nmat, const dg_device_texmap* texmaps, uint32_t ntex, void* bgra_out,
+                            void* depth_out, void* stream, int32_t* status_out);
+
 #ifdef __cplusplus
 }
 #endif
