@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--batch-frames", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     return ap.parse_args()
@@ -388,6 +391,9 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_batch:
         line["batched"] = batched_leg(ctx, stream, args.batch_frames)
 
+    if rank == 0 and world == 1 and not args.no_serve:
+        line["served"] = serving_leg(local, seconds=args.serve_seconds, rate=args.serve_rate)
+
     if rank == 0 and world == 1 and not args.no_cpu:
         bgra, depth = canvas.read()
         threads = os.cpu_count() or 1
@@ -448,6 +454,150 @@ def batched_leg(ctx, stream, n_frames: int) -> dict:
            "workload": "256 frames, side log-uniform 128..512, 1k..200k triangles (torus/sphere), "
                        "textures 256^2..1024^2 from a pool of 32; L2 not flushed (working set > L2)"}
     return out
+
+
+SERVE_RES = [(256, 256), (512, 512), (1920, 1080), (3840, 2160)]
+SERVE_P = [0.4, 0.3, 0.2, 0.1]
+
+
+def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes: int = 64, n_tex: int = 32,
+                budget: int = 40 << 30, seed: int = 1234) -> dict:
+    """Serving workload: Poisson request stream against a resident pool of meshes
+    and textures, served by the continuous-batching server (dg_server_*), next to
+    the plain one-frame-per-launch path on the same request mix."""
+    import threading as th
+
+    import numpy as np
+    import torch
+
+    from draw_gb300 import renderer as R
+    from draw_gb300 import scenes as S
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t0 = time.perf_counter()
+    ctx = R.Context(local)
+    tms = [R.TextureMap(*(lambda t: (t.img, t.width, t.height, t.comps))(S.value_noise_checker(512, 512, seed + i)),
+                        ctx=ctx) for i in range(n_tex)]
+    objs, ntris = [], []
+    for i in range(n_meshes):
+        nt = int(round(math.exp(rng.uniform(math.log(5_000), math.log(2_000_000)))))
+        pos, nrm, uv, tri = S.mesh_for_tris("torus" if i % 2 == 0 else "sphere", nt)
+        mat = S.Material((0.1,) * 3, (0.7,) * 3, (0.2,) * 3, 1.0, 0, 0)
+        objs.append(R.upload_object(S.ObjectDesc(pos, nrm, uv, [S.MeshDesc(S._tris9(tri), 0)], [mat]),
+                                    [tms[i % n_tex]], ctx))
+        ntris.append(tri.shape[0])
+    gen_s = time.perf_counter() - t0
+
+    def sample(n):
+        out = []
+        for _ in range(n):
+            w, h = SERVE_RES[int(rng.choice(4, p=SERVE_P))]
+            oi = int(rng.integers(0, n_meshes))
+            az, el, d = rng.uniform(0, 2 * math.pi), rng.uniform(0.1, 1.0), rng.uniform(2.6, 4.0)
+            cam = (d * math.cos(el) * math.sin(az), d * math.sin(el), d * math.cos(el) * math.cos(az))
+            light = [(3.0 * math.sin(az + 1), 4.0, 3.0 * math.cos(az + 1))]
+            out.append((oi, w, h, cam, light))
+        return out
+
+    # 1) plain path: one Scene::render call (one launch sequence) per request, back to back
+    plain_reqs = sample(400)
+    scenes, canvases = {}, {}
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    for oi, w, h, cam, light in plain_reqs:
+        if (oi, w, h) not in scenes:
+            sc = R.Scene(w, h, ctx)
+            sc.add_obj(objs[oi])
+            scenes[(oi, w, h)] = sc
+        if (w, h) not in canvases:
+            cv = R.Canvas(w, h, ctx)
+            cv.init_depth(float("inf"))
+            canvases[(w, h)] = cv
+
+    def run_plain():
+        for oi, w, h, cam, light in plain_reqs:
+            sc = scenes[(oi, w, h)]
+            sc.camera.reset(cam, tuple(-c for c in cam), float(np.float32(w) / np.float32(h)), -0.5, -100.0, 60.0)
+            sc.set_lights(light)
+            sc.render(canvases[(w, h)])
+
+    with torch.cuda.stream(stream):
+        run_plain()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        e0.record(stream)
+        run_plain()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_wall = time.perf_counter() - w0
+    plain_dev = e0.elapsed_time(e1) / 1e3
+    ctx.set_stream(None)
+
+    srv = R.Server(ctx, budget_bytes=budget, max_batch=64, streams=3)
+
+    def req(q):
+        oi, w, h, cam, light = q
+        return R.Server.request(objs[oi], w, h, cam, tuple(-c for c in cam), -0.5, -100.0, 60.0, light,
+                                discard=True)
+
+    # 2) saturated: the whole mix submitted at once
+    sat_reqs = [req(q) for q in sample(1500)]
+    for t in [srv.submit(r) for r in sat_reqs[:200]]:
+        srv.wait(t)
+    srv.reset_stats()
+    w0 = time.perf_counter()
+    tickets = [srv.submit(r) for r in sat_reqs]
+    for t in tickets:
+        srv.wait(t)
+    sat_s = time.perf_counter() - w0
+    sat_stats = srv.stats()
+
+    # 3) Poisson arrivals at `rate` for `seconds`
+    n = int(rate * seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    pois_reqs = [req(q) for q in sample(n)]
+    srv.reset_stats()
+    tq = []
+    done = th.Event()
+
+    def waiter():
+        i = 0
+        while i < n:
+            if i < len(tq):
+                srv.wait(tq[i])
+                i += 1
+            else:
+                time.sleep(0.0002)
+        done.set()
+
+    wt = th.Thread(target=waiter)
+    wt.start()
+    start = time.perf_counter()
+    for k in range(n):
+        delay = start + arrivals[k] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        tq.append(srv.submit(pois_reqs[k]))
+    submit_span = time.perf_counter() - start
+    wt.join()
+    total_span = time.perf_counter() - start
+    ps = srv.stats()
+    srv.close()
+    ctx.close()
+    return {
+        "workload": f"Poisson {rate:.0f} req/s for {seconds:.0f} s; resolution {SERVE_RES} with p={SERVE_P}; "
+                    f"{n_meshes} resident meshes of 5k..2M triangles (log-uniform, {sum(ntris) / 1e6:.1f}M total), "
+                    f"{n_tex} resident 512^2 textures; budget {budget / 2**30:.0f} GiB; max batch 64, 3 streams",
+        "pool_build_s": gen_s,
+        "plain_frames_per_s": len(plain_reqs) / plain_dev, "plain_wall_frames_per_s": len(plain_reqs) / plain_wall,
+        "saturated_frames_per_s": len(sat_reqs) / sat_s, "saturated_mean_batch": sat_stats["mean_batch"],
+        "saturated_vs_plain": (len(sat_reqs) / sat_s) / (len(plain_reqs) / plain_dev),
+        "offered_rps": n / arrivals[-1], "achieved_frames_per_s": n / total_span, "submit_span_s": submit_span,
+        "p50_ms": ps["p50_ms"], "p99_ms": ps["p99_ms"], "max_ms": ps["max_ms"],
+        "p99_over_p50": ps["p99_ms"] / ps["p50_ms"] if ps["p50_ms"] else None, "mean_batch": ps["mean_batch"],
+        "peak_gib": ps["peak_bytes"] / 2**30, "errors": ps["error"],
+    }
 
 
 _TRAFFIC = None

@@ -10,33 +10,15 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
-#include <mutex>
 #include <new>
 #include <vector>
 
-#include "dg_internal.cuh"
+#include "dg_host.h"
+
+namespace dgh {
 
 namespace {
 
-// ------------------------------------------------------------ host vectors
-struct HV3 {
-    float x, y, z;
-};
-inline HV3 h3(float x, float y, float z) { return HV3{x, y, z}; }
-inline HV3 hadd(HV3 a, HV3 b) { return h3(a.x + b.x, a.y + b.y, a.z + b.z); }
-inline HV3 hsub(HV3 a, HV3 b) { return h3(a.x - b.x, a.y - b.y, a.z - b.z); }
-inline HV3 hmul(HV3 a, float s) { return h3(a.x * s, a.y * s, a.z * s); }
-inline HV3 hdiv(HV3 a, float s) { return h3(a.x / s, a.y / s, a.z / s); }
-inline float hdot(HV3 a, HV3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }           // linalg.rs:182-184
-inline float hnorm(HV3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }      // linalg.rs:167-171
-inline HV3 hnormalized(HV3 a) { return hdiv(a, hnorm(a)); }                               // linalg.rs:173-175
-inline HV3 hcross(HV3 a, HV3 b) {                                                          // linalg.rs:186-200
-    return h3((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x));
-}
-
-struct HM4 {
-    float m[4][4];
-};
 HM4 hm_zero() {
     HM4 r;
     std::memset(&r, 0, sizeof(r));
@@ -62,12 +44,20 @@ void hm_vec(const HM4& a, const float v[4], float out[4]) {  // linalg.rs:346-36
 
 const float kRadsPerDeg = 3.14159265358979323846f / 180.0f;  // f32::to_radians
 
-struct Camera {  // scene/mod.rs:282-294
-    HV3 position, direction, up;
-    float top, bottom, right, left;
-    float near_, far_;
-    HV3 u, v, w;
-};
+dg_status camera_basis(const Camera& c, HM4& b) {  // scene/mod.rs:415-428
+    if (!(hnorm(c.u) > 0.0f && hnorm(c.v) > 0.0f && hnorm(c.w) > 0.0f)) return DG_E_CAMERA;
+    b = hm_zero();
+    const HV3 cols[3] = {c.u, c.v, c.w};
+    for (int j = 0; j < 3; j++) {
+        b.m[0][j] = cols[j].x;
+        b.m[1][j] = cols[j].y;
+        b.m[2][j] = cols[j].z;
+    }
+    b.m[3][3] = 1.0f;
+    return DG_OK;
+}
+
+}  // namespace
 
 dg_status camera_init(Camera& c, HV3 pos, HV3 dir, float ratio, float near_, float far_, float fov_x) {
     // Camera::new, scene/mod.rs:297-357
@@ -102,33 +92,47 @@ void camera_update_basis(Camera& c) {  // scene/mod.rs:438-451
     c.w = hnormalized(w);
 }
 
-dg_status camera_basis(const Camera& c, HM4& b) {  // scene/mod.rs:415-428
-    if (!(hnorm(c.u) > 0.0f && hnorm(c.v) > 0.0f && hnorm(c.w) > 0.0f)) return DG_E_CAMERA;
-    b = hm_zero();
-    const HV3 cols[3] = {c.u, c.v, c.w};
-    for (int j = 0; j < 3; j++) {
-        b.m[0][j] = cols[j].x;
-        b.m[1][j] = cols[j].y;
-        b.m[2][j] = cols[j].z;
+dg_status camera_op(Scene& s, int32_t op, const float* a) {
+    Camera& cam = s.cam;
+    switch (op) {
+        case 0: cam.position = hadd(cam.position, hmul(cam.up, a[0])); break;   // move_up :381-383
+        case 1: cam.position = hadd(cam.position, hmul(cam.up, -a[0])); break;  // move_down :385-387
+        case 2: cam.position = hadd(cam.position, hmul(cam.u, -a[0])); break;   // move_left :389-391
+        case 3: cam.position = hadd(cam.position, hmul(cam.u, a[0])); break;    // move_right :393-395
+        case 4: cam.position = hadd(cam.position, hmul(hnormalized(hcross(cam.up, cam.u)), a[0])); break;  // :397-400
+        case 5: cam.position = hadd(cam.position, hmul(hnormalized(hcross(cam.u, cam.up)), a[0])); break;  // :402-405
+        case 6: {  // rotate_origin: Matrix4::rotate_y(theta.to_radians()) * v.as_vec4(), :407-413
+            float th = a[0] * kRadsPerDeg;
+            float sn = std::sin(th), cs = std::cos(th);
+            HM4 r = hm_zero();
+            r.m[0][0] = cs; r.m[0][2] = sn; r.m[1][1] = 1.0f; r.m[2][0] = -sn; r.m[2][2] = cs; r.m[3][3] = 1.0f;
+            float p[4] = {cam.position.x, cam.position.y, cam.position.z, 1.0f}, po[4];
+            float d[4] = {cam.direction.x, cam.direction.y, cam.direction.z, 1.0f}, dout[4];
+            hm_vec(r, p, po);
+            hm_vec(r, d, dout);
+            cam.position = h3(po[0], po[1], po[2]);
+            cam.direction = h3(dout[0], dout[1], dout[2]);
+            break;
+        }
+        case 7: cam.position = h3(a[0], a[1], a[2]); break;  // set_pos :377-379
+        case 8: {                                             // Scene::move_camera_direction :803-813
+            int32_t dx = (int32_t)a[0], dy = (int32_t)a[1];
+            if (!((int64_t)dx < (int64_t)s.width) || !((int64_t)dy < (int64_t)s.height)) return DG_E_INVALID;
+            float fx = (float)dx / (float)s.width, fy = (float)dy / (float)s.height;
+            cam.direction = hnormalized(hadd(hadd(cam.direction, hmul(cam.u, fx)), hmul(cam.v, fy)));  // :430-432
+            camera_update_basis(cam);
+            break;
+        }
+        default: return DG_E_INVALID;
     }
-    b.m[3][3] = 1.0f;
     return DG_OK;
 }
 
-struct Scene {  // scene/mod.rs:749-757
-    uint64_t width, height;
-    Camera cam;
-    std::vector<int32_t> objects;
-    std::vector<HV3> lights;
-    int32_t exponent;
-};
-
-// gen_transformation_matrix (scene/mod.rs:817-899) and gen_view_planes (:481-593).
 dg_status frame_setup(Scene& s, float M[4][4], float planes[6][4]) {
     Camera& c = s.cam;
     const float nx = (float)s.width, ny = (float)s.height;
     const float n = c.near_, f = c.far_, r = c.right, l = c.left, t = c.top, b = c.bottom;
-    // Camera::gen_matrix, :453-479
+    // Camera::gen_matrix, scene/mod.rs:453-479
     HM4 tr = hm_zero();
     tr.m[0][0] = tr.m[1][1] = tr.m[2][2] = tr.m[3][3] = 1.0f;
     tr.m[0][3] = -c.position.x;
@@ -166,7 +170,7 @@ dg_status frame_setup(Scene& s, float M[4][4], float planes[6][4]) {
     HM4 full = hm_mul(hm_mul(hm_mul(vp, orth), persp), view);
     std::memcpy(M, full.m, sizeof(full.m));
 
-    // view planes
+    // Camera::gen_view_planes, scene/mod.rs:481-593
     camera_update_basis(c);
     e = camera_basis(c, basis);
     if (e) return e;
@@ -182,7 +186,7 @@ dg_status frame_setup(Scene& s, float M[4][4], float planes[6][4]) {
     HV3 vis = hdiv(hadd(urn, lcf), 2.0f);
     const HV3 pts[6][3] = {{urn, lrn, lln}, {lfc, rcf, ucf}, {rcf, urn, lrn},
                            {lfc, lln, uln}, {ucf, uln, urn}, {lcf, lln, lrn}};
-    for (int p = 0; p < 6; p++) {  // ViewPlane::new, :603-632
+    for (int p = 0; p < 6; p++) {  // ViewPlane::new, scene/mod.rs:603-632
         HV3 pv = hsub(pts[p][1], pts[p][0]);
         HV3 qv = hsub(pts[p][2], pts[p][1]);
         HV3 nn = hcross(pv, qv);
@@ -202,89 +206,19 @@ dg_status frame_setup(Scene& s, float M[4][4], float planes[6][4]) {
     return DG_OK;
 }
 
-// ------------------------------------------------------------- resources
-struct TexMap {
-    uint32_t* d_words = nullptr;
-    uint64_t len = 0;
-    uint32_t w = 0, h = 0, comps = 0;
-};
+}  // namespace dgh
 
-struct Object {
-    bool alive = false;
-    float4* d_pos = nullptr;
-    float4* d_nrm = nullptr;
-    float2* d_uv = nullptr;
-    uint4* d_tri_pos = nullptr;
-    uint4* d_tri_uv = nullptr;
-    uint4* d_tri_nrm = nullptr;
-    DgMatDev* d_mats = nullptr;
-    uint32_t nv = 0, nn = 0, nuv = 0, ntri_opaque = 0, nmats = 0;
-    std::vector<float> h_pos;                        // for the transparent pass sort
-    std::vector<std::vector<uint32_t>> transparent;  // 9 indices per triangle, current order
-    std::vector<int32_t> transparent_mat;
-};
-
-struct Canvas {
-    bool alive = false;
-    uint64_t w = 0, h = 0;
-    uint32_t* d_colour = nullptr;
-    float* d_depth = nullptr;
-    uint64_t* d_vis = nullptr;
-    bool depth_init = false;
-    float depth_max = 0.0f;
-    float off_x = 0.0f, off_y = 0.0f;
-};
-
-}  // namespace
-
-struct dg_ctx {
-    int device = 0;
-    int nsm = 152;
-    cudaStream_t stream = nullptr;
-    cudaStream_t own_stream = nullptr;
-    std::vector<TexMap> tex;  // [0] = 1x1 white default map
-    DgTexDev* d_tex = nullptr;
-    size_t d_tex_cap = 0;
-    bool tex_dirty = true;
-    std::vector<Object> objects;
-    std::vector<Scene> scenes;
-    std::vector<Canvas> canvases;
-    // render scratch
-    float4* d_vrec = nullptr;
-    size_t vrec_cap = 0;
-    float4* d_vshade = nullptr;
-    size_t vshade_cap = 0;
-    uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
-    size_t vmark_cap = 0;
-    DgQueueRec* d_queue = nullptr;
-    uint32_t* d_queue_base = nullptr;
-    size_t queue_cap = 0;
-    uint32_t small_max_px = DG_SMALL_MAX_PX;
-    unsigned long long* d_counters = nullptr;  // [0] queue counter, [1] covered px, [2] overflow
-    uint32_t* d_err = nullptr;
-    // job descriptors: pinned staging ring + device copies
-    static const int kSlots = 4;
-    void* h_stage[kSlots] = {};
-    void* d_stage[kSlots] = {};
-    size_t stage_cap[kSlots] = {};
-    cudaEvent_t stage_ev[kSlots] = {};
-    int slot = 0;
-    // timing
-    bool timing = false;
-    cudaEvent_t ev[5] = {};
-    bool ev_valid = false;
-    uint64_t last_vtx = 0, last_tri = 0, last_h2d = 0, last_launches = 0;
-};
+using namespace dgh;
 
 namespace {
 
 dg_status cuda_ok(cudaError_t e) { return e == cudaSuccess ? DG_OK : DG_E_CUDA; }
-#define DG_CUDA(x)                                      \
-    do {                                                \
-        cudaError_t _e = (x);                           \
-        if (_e != cudaSuccess) {                        \
+#define DG_CUDA(x)                                                         \
+    do {                                                                   \
+        cudaError_t _e = (x);                                              \
+        if (_e != cudaSuccess) {                                           \
             return _e == cudaErrorMemoryAllocation ? DG_E_OOM : DG_E_CUDA; \
-        }                                               \
+        }                                                                  \
     } while (0)
 
 template <class T>
@@ -305,13 +239,7 @@ void dfree(T*& p) {
     p = nullptr;
 }
 
-dg_status set_device(dg_ctx* c) {
-    if (c->device < 0) return DG_E_CUDA;  // host-only context: no device work
-    return cuda_ok(cudaSetDevice(c->device));
-}
-
-dg_status tex_upload(dg_ctx* c, const uint8_t* img, uint64_t len, uint32_t w, uint32_t h, uint32_t comps,
-                     TexMap& out) {
+dg_status tex_upload(const uint8_t* img, uint64_t len, uint32_t w, uint32_t h, uint32_t comps, TexMap& out) {
     uint64_t nwords = (len + 3) / 4 + 1;
     std::vector<uint32_t> words(nwords, 0u);
     if (len) std::memcpy(words.data(), img, len);
@@ -325,37 +253,12 @@ dg_status tex_upload(dg_ctx* c, const uint8_t* img, uint64_t len, uint32_t w, ui
     return DG_OK;
 }
 
-dg_status sync_tex_table(dg_ctx* c) {
-    if (!c->tex_dirty) return DG_OK;
-    std::vector<DgTexDev> t(c->tex.size());
-    for (size_t i = 0; i < c->tex.size(); i++) {
-        t[i].words = c->tex[i].d_words;
-        t[i].len = c->tex[i].len;
-        t[i].width = c->tex[i].w;
-        t[i].height = c->tex[i].h;
-        t[i].comps = c->tex[i].comps;
-        t[i].fw = (float)c->tex[i].w;
-        t[i].fh = (float)c->tex[i].h;
-    }
-    if (c->d_tex_cap < t.size()) {
-        DG_CUDA(cudaStreamSynchronize(c->stream));
-        dfree(c->d_tex);
-        size_t cap = std::max<size_t>(16, t.size() * 2);
-        dg_status e = dalloc(&c->d_tex, cap);
-        if (e) return e;
-        c->d_tex_cap = cap;
-    } else {
-        DG_CUDA(cudaStreamSynchronize(c->stream));
-    }
-    DG_CUDA(cudaMemcpy(c->d_tex, t.data(), t.size() * sizeof(DgTexDev), cudaMemcpyHostToDevice));
-    c->tex_dirty = false;
-    return DG_OK;
-}
-
+// Grows a slot scratch buffer (synchronizing only that slot's stream).
 template <class T>
-dg_status grow(dg_ctx* c, T** p, size_t* cap, size_t need) {
+dg_status grow(JobSlot& s, T** p, size_t* cap, size_t need) {
     if (*cap >= need && *p) return DG_OK;
-    DG_CUDA(cudaStreamSynchronize(c->stream));
+    DG_CUDA(cudaStreamSynchronize(s.stream));
+    if (*p) s.scratch_bytes -= *cap * sizeof(T);
     dfree(*p);
     size_t n = std::max(need, (size_t)(*cap * 3 / 2));
     dg_status e = dalloc(p, n);
@@ -364,6 +267,7 @@ dg_status grow(dg_ctx* c, T** p, size_t* cap, size_t need) {
         return e;
     }
     *cap = n;
+    s.scratch_bytes += n * sizeof(T);
     return DG_OK;
 }
 
@@ -380,19 +284,126 @@ Object* get_object(dg_ctx* c, int32_t id) {
     return &c->objects[id];
 }
 
-dg_status take_errors(dg_ctx* c) {
+// dg_scene_render / dg_render_batch: resolves ids, then launches on the context slot.
+dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n) {
+    if (n == 0) return DG_OK;
+    std::vector<Scene*> sc(n);
+    std::vector<FrameTarget> tg(n);
+    for (uint32_t i = 0; i < n; i++) {
+        Scene* s = get_scene(c, scenes[i]);
+        Canvas* cv = get_canvas(c, canvases[i]);
+        if (!s || !cv) return DG_E_INVALID;
+        if (!cv->depth_init) return DG_E_DEPTH_UNINIT;
+        sc[i] = s;
+        tg[i] = FrameTarget{cv->d_colour, cv->d_depth, cv->d_vis, cv->w, cv->h, cv->depth_max, cv->off_x, cv->off_y};
+    }
+    return launch_frames(c, c->main, sc.data(), tg.data(), n);
+}
+
+}  // namespace
+
+namespace dgh {
+
+dg_status set_device(dg_ctx* c) {
+    if (c->device < 0) return DG_E_CUDA;  // host-only context: no device work
+    return cuda_ok(cudaSetDevice(c->device));
+}
+
+dg_status slot_init(dg_ctx* c, JobSlot& s, cudaStream_t stream) {
+    (void)c;
+    s.stream = stream;
+    for (int i = 0; i < JobSlot::kStage; i++) DG_CUDA(cudaEventCreateWithFlags(&s.stage_ev[i], cudaEventDisableTiming));
+    for (int i = 0; i < 5; i++) DG_CUDA(cudaEventCreate(&s.ev[i]));
+    dg_status e = dalloc(&s.d_counters, 4);
+    if (e) return e;
+    e = dalloc(&s.d_err, 1);
+    if (e) return e;
+    DG_CUDA(cudaMemset(s.d_err, 0, 4));
+    return DG_OK;
+}
+
+void slot_free(JobSlot& s) {
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    dfree(s.d_vrec);
+    dfree(s.d_vshade);
+    dfree(s.d_vmark);
+    dfree(s.d_queue);
+    dfree(s.d_queue_base);
+    dfree(s.d_counters);
+    dfree(s.d_err);
+    for (int i = 0; i < JobSlot::kStage; i++) {
+        if (s.h_stage[i]) cudaFreeHost(s.h_stage[i]);
+        s.h_stage[i] = nullptr;
+        dfree(s.d_stage[i]);
+        if (s.stage_ev[i]) cudaEventDestroy(s.stage_ev[i]);
+        s.stage_ev[i] = nullptr;
+    }
+    for (int i = 0; i < 5; i++) {
+        if (s.ev[i]) cudaEventDestroy(s.ev[i]);
+        s.ev[i] = nullptr;
+    }
+    s.scratch_bytes = 0;
+}
+
+dg_status slot_take_errors(JobSlot& s) {
     uint32_t err = 0;
-    DG_CUDA(cudaMemcpy(&err, c->d_err, 4, cudaMemcpyDeviceToHost));
+    DG_CUDA(cudaMemcpy(&err, s.d_err, 4, cudaMemcpyDeviceToHost));
     if (!err) return DG_OK;
     uint32_t zero = 0;
-    DG_CUDA(cudaMemcpy(c->d_err, &zero, 4, cudaMemcpyHostToDevice));
+    DG_CUDA(cudaMemcpy(s.d_err, &zero, 4, cudaMemcpyHostToDevice));
     for (int b = 1; b < 32; b++)
         if (err & (1u << b)) return (dg_status)b;
     return DG_E_CUDA;
 }
 
-// Builds and launches one render job over n (scene, canvas) frames.
-dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n) {
+dg_status sync_tex_table(dg_ctx* c, cudaStream_t stream) {
+    if (!c->tex_dirty) return DG_OK;
+    std::vector<DgTexDev> t(c->tex.size());
+    for (size_t i = 0; i < c->tex.size(); i++) {
+        t[i].words = c->tex[i].d_words;
+        t[i].len = c->tex[i].len;
+        t[i].width = c->tex[i].w;
+        t[i].height = c->tex[i].h;
+        t[i].comps = c->tex[i].comps;
+        t[i].fw = (float)c->tex[i].w;
+        t[i].fh = (float)c->tex[i].h;
+    }
+    DG_CUDA(cudaStreamSynchronize(stream));
+    if (c->d_tex_cap < t.size()) {
+        DG_CUDA(cudaDeviceSynchronize());  // the old table may still be read by other streams
+        dfree(c->d_tex);
+        size_t cap = std::max<size_t>(16, t.size() * 2);
+        dg_status e = dalloc(&c->d_tex, cap);
+        if (e) return e;
+        c->d_tex_cap = cap;
+    }
+    DG_CUDA(cudaMemcpy(c->d_tex, t.data(), t.size() * sizeof(DgTexDev), cudaMemcpyHostToDevice));
+    c->tex_dirty = false;
+    return DG_OK;
+}
+
+// Queue capacity: one record per input triangle (clip outputs beyond it, and
+// anything past 2^24 records, are rasterized in place by their warp).
+size_t queue_records(uint64_t total_tri) {
+    return std::min<size_t>(std::max<size_t>(1u << 16, (size_t)total_tri), (1u << 24) - 1);
+}
+
+uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L) {
+    auto cap_after = [](size_t cap, const void* p, size_t need) -> size_t {
+        return (cap >= need && p) ? cap : std::max(need, cap * 3 / 2);
+    };
+    if (L == 0) L = 1;
+    const size_t vrec = cap_after(s.vrec_cap, s.d_vrec, std::max<uint64_t>(V, 1));
+    const size_t vshade = cap_after(s.vshade_cap, s.d_vshade, std::max<uint64_t>(V * L * 2, 1));
+    const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>((V + 31) / 32, 1));
+    const size_t q = cap_after(s.queue_cap, s.d_queue, queue_records(T));
+    const size_t qb = (s.queue_cap >= queue_records(T) && s.d_queue) ? s.queue_base_cap
+                                                                     : cap_after(s.queue_base_cap, s.d_queue_base, q);
+    return vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + q * sizeof(DgQueueRec) +
+           qb * sizeof(uint32_t);
+}
+
+dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n) {
     if (n == 0) return DG_OK;
     dg_status e = set_device(c);
     if (e) return e;
@@ -401,41 +412,41 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
     uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0;
     uint32_t stride = 1;
     for (uint32_t i = 0; i < n; i++) {
-        Scene* s = get_scene(c, scenes[i]);
-        Canvas* cv = get_canvas(c, canvases[i]);
-        if (!s || !cv) return DG_E_INVALID;
-        if (!cv->depth_init) return DG_E_DEPTH_UNINIT;
-        for (int32_t oid : s->objects)
+        Scene& s = *scenes[i];  // frame_setup updates the camera basis, as Scene::render does
+        const FrameTarget& tg = targets[i];
+        for (int32_t oid : s.objects)
+            if (oid < 0 || (size_t)oid >= c->objects.size() || !c->objects[oid].alive) return DG_E_INVALID;
+        for (int32_t oid : s.objects)
             if (!c->objects[oid].transparent.empty()) return DG_E_LIMIT;
         DgFrameDev& f = frames[i];
         std::memset(&f, 0, sizeof(f));
-        e = frame_setup(*s, f.M, f.plane);
+        e = frame_setup(s, f.M, f.plane);
         if (e) return e;
-        f.cam[0] = s->cam.position.x;
-        f.cam[1] = s->cam.position.y;
-        f.cam[2] = s->cam.position.z;
-        f.clear_depth = cv->depth_max;
-        f.nlights = (uint32_t)s->lights.size();
-        for (size_t l = 0; l < s->lights.size(); l++) {
-            f.light[l][0] = s->lights[l].x;
-            f.light[l][1] = s->lights[l].y;
-            f.light[l][2] = s->lights[l].z;
+        f.cam[0] = s.cam.position.x;
+        f.cam[1] = s.cam.position.y;
+        f.cam[2] = s.cam.position.z;
+        f.clear_depth = tg.clear_depth;
+        f.nlights = (uint32_t)s.lights.size();
+        for (size_t l = 0; l < s.lights.size(); l++) {
+            f.light[l][0] = s.lights[l].x;
+            f.light[l][1] = s.lights[l].y;
+            f.light[l][2] = s.lights[l].z;
         }
         stride = std::max(stride, f.nlights);
-        f.exponent = s->exponent;
-        f.off_x = cv->off_x;
-        f.off_y = cv->off_y;
-        f.width = (uint32_t)cv->w;
-        f.height = (uint32_t)cv->h;
-        f.vis = cv->d_vis;
-        f.colour = cv->d_colour;
-        f.depth = cv->d_depth;
+        f.exponent = s.exponent;
+        f.off_x = tg.off_x;
+        f.off_y = tg.off_y;
+        f.width = (uint32_t)tg.w;
+        f.height = (uint32_t)tg.h;
+        f.vis = tg.vis;
+        f.colour = tg.colour;
+        f.depth = tg.depth;
         f.seg_begin = (uint32_t)segs.size();
         f.tile_begin = (uint32_t)total_tiles;
-        f.tiles_x = (uint32_t)((cv->w + DG_TILE_W - 1) / DG_TILE_W);
-        total_tiles += (uint64_t)f.tiles_x * ((cv->h + DG_TILE_H - 1) / DG_TILE_H);
+        f.tiles_x = (uint32_t)((tg.w + DG_TILE_W - 1) / DG_TILE_W);
+        total_tiles += (uint64_t)f.tiles_x * ((tg.h + DG_TILE_H - 1) / DG_TILE_H);
         uint64_t seq = 0;
-        for (int32_t oid : s->objects) {
+        for (int32_t oid : s.objects) {
             Object& o = c->objects[oid];
             DgSegDev sg;
             std::memset(&sg, 0, sizeof(sg));
@@ -467,98 +478,91 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
         std::memset(&sg, 0, sizeof(sg));
         segs.push_back(sg);
     }
-    e = sync_tex_table(c);
+    e = sync_tex_table(c, S.stream);
     if (e) return e;
-    e = grow(c, &c->d_vrec, &c->vrec_cap, std::max<uint64_t>(total_vtx, 1));
+    e = grow(S, &S.d_vrec, &S.vrec_cap, std::max<uint64_t>(total_vtx, 1));
     if (e) return e;
-    e = grow(c, &c->d_vshade, &c->vshade_cap, std::max<uint64_t>(total_vtx * stride * 2, 1));
+    e = grow(S, &S.d_vshade, &S.vshade_cap, std::max<uint64_t>(total_vtx * stride * 2, 1));
     if (e) return e;
     const size_t want_mark = std::max<uint64_t>((total_vtx + 31) / 32, 1);
-    if (c->vmark_cap < want_mark) {
-        e = grow(c, &c->d_vmark, &c->vmark_cap, want_mark);
+    if (S.vmark_cap < want_mark) {
+        e = grow(S, &S.d_vmark, &S.vmark_cap, want_mark);
         if (e) return e;
-        DG_CUDA(cudaMemsetAsync(c->d_vmark, 0, c->vmark_cap * sizeof(uint32_t), c->stream));
+        DG_CUDA(cudaMemsetAsync(S.d_vmark, 0, S.vmark_cap * sizeof(uint32_t), S.stream));
     }
-    // Queue capacity: every input triangle may produce up to 4 queued clip outputs; the
-    // cap keeps the scratch bounded (overflowing triangles are rasterized in place).
-    size_t want_queue = std::min<size_t>(std::max<size_t>(1u << 16, (size_t)total_tri), (1u << 24) - 1);
-    if (c->queue_cap < want_queue) {
-        DG_CUDA(cudaStreamSynchronize(c->stream));
-        dfree(c->d_queue);
-        dfree(c->d_queue_base);
-        c->queue_cap = 0;
-        e = dalloc(&c->d_queue, want_queue);
+    const size_t want_queue = queue_records(total_tri);
+    if (S.queue_cap < want_queue) {
+        e = grow(S, &S.d_queue, &S.queue_cap, want_queue);
         if (e) return e;
-        e = dalloc(&c->d_queue_base, want_queue);
+        e = grow(S, &S.d_queue_base, &S.queue_base_cap, S.queue_cap);
         if (e) return e;
-        c->queue_cap = want_queue;
     }
 
     // job descriptor upload through a pinned staging slot
-    size_t fbytes = frames.size() * sizeof(DgFrameDev), sbytes = segs.size() * sizeof(DgSegDev);
-    size_t need = fbytes + sbytes;
-    int slot = c->slot;
-    c->slot = (c->slot + 1) % dg_ctx::kSlots;
-    DG_CUDA(cudaEventSynchronize(c->stage_ev[slot]));
-    if (c->stage_cap[slot] < need) {
-        if (c->h_stage[slot]) cudaFreeHost(c->h_stage[slot]);
-        dfree(c->d_stage[slot]);
-        c->h_stage[slot] = nullptr;
-        c->stage_cap[slot] = 0;
+    const size_t fbytes = frames.size() * sizeof(DgFrameDev), sbytes = segs.size() * sizeof(DgSegDev);
+    const size_t need = fbytes + sbytes;
+    const int k = S.stage;
+    S.stage = (S.stage + 1) % JobSlot::kStage;
+    DG_CUDA(cudaEventSynchronize(S.stage_ev[k]));
+    if (S.stage_cap[k] < need) {
+        if (S.h_stage[k]) cudaFreeHost(S.h_stage[k]);
+        dfree(S.d_stage[k]);
+        S.h_stage[k] = nullptr;
+        S.stage_cap[k] = 0;
         size_t cap = std::max<size_t>(need * 2, 64 * 1024);
-        DG_CUDA(cudaMallocHost(&c->h_stage[slot], cap));
-        e = dalloc((uint8_t**)&c->d_stage[slot], cap);
+        DG_CUDA(cudaMallocHost(&S.h_stage[k], cap));
+        e = dalloc((uint8_t**)&S.d_stage[k], cap);
         if (e) return e;
-        c->stage_cap[slot] = cap;
+        S.stage_cap[k] = cap;
     }
-    std::memcpy(c->h_stage[slot], frames.data(), fbytes);
-    std::memcpy((uint8_t*)c->h_stage[slot] + fbytes, segs.data(), sbytes);
-    DG_CUDA(cudaMemcpyAsync(c->d_stage[slot], c->h_stage[slot], need, cudaMemcpyHostToDevice, c->stream));
-    DG_CUDA(cudaEventRecord(c->stage_ev[slot], c->stream));
+    std::memcpy(S.h_stage[k], frames.data(), fbytes);
+    std::memcpy((uint8_t*)S.h_stage[k] + fbytes, segs.data(), sbytes);
+    DG_CUDA(cudaMemcpyAsync(S.d_stage[k], S.h_stage[k], need, cudaMemcpyHostToDevice, S.stream));
+    DG_CUDA(cudaEventRecord(S.stage_ev[k], S.stream));
 
     DgJobDev job;
     std::memset(&job, 0, sizeof(job));
-    job.frames = (const DgFrameDev*)c->d_stage[slot];
-    job.segs = (const DgSegDev*)((uint8_t*)c->d_stage[slot] + fbytes);
+    job.frames = (const DgFrameDev*)S.d_stage[k];
+    job.segs = (const DgSegDev*)((uint8_t*)S.d_stage[k] + fbytes);
     job.nframes = n;
     job.nsegs = (uint32_t)segs.size();
     job.total_vtx = (uint32_t)total_vtx;
     job.total_tri = (uint32_t)total_tri;
     job.total_tiles = (uint32_t)total_tiles;
     job.shade_stride = stride;
-    job.vrec = c->d_vrec;
-    job.vshade = c->d_vshade;
-    job.vmark = c->d_vmark;
-    job.queue = c->d_queue;
-    job.queue_base = c->d_queue_base;
-    job.queue_cap = (uint32_t)std::min<size_t>(c->queue_cap, (1u << 24) - 1);
-    job.small_max_px = c->small_max_px;
-    job.queue_counter = c->d_counters;
-    job.stats = c->d_counters + 1;
+    job.vrec = S.d_vrec;
+    job.vshade = S.d_vshade;
+    job.vmark = S.d_vmark;
+    job.queue = S.d_queue;
+    job.queue_base = S.d_queue_base;
+    job.queue_cap = (uint32_t)std::min<size_t>(S.queue_cap, (1u << 24) - 1);
+    job.small_max_px = S.small_max_px;
+    job.queue_counter = S.d_counters;
+    job.stats = S.d_counters + 1;
     job.tex = c->d_tex;
-    job.err = c->d_err;
-    c->last_vtx = total_vtx;
-    c->last_tri = total_tri;
-    c->last_h2d = need;
-    c->last_launches = (total_vtx ? 1 : 0) + (total_tri ? 2 : 0) + (total_tiles ? 1 : 0);
+    job.err = S.d_err;
+    S.last_vtx = total_vtx;
+    S.last_tri = total_tri;
+    S.last_h2d = need;
+    S.last_launches = (total_vtx ? 1 : 0) + (total_tri ? 2 : 0) + (total_tiles ? 1 : 0);
 
-    DG_CUDA(cudaMemsetAsync(c->d_counters, 0, 3 * sizeof(unsigned long long), c->stream));
-    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[0], c->stream));
-    DG_CUDA(dg_launch_vertex(job, c->stream));
-    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[1], c->stream));
-    DG_CUDA(dg_launch_setup_raster(job, c->nsm, c->stream));
-    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[2], c->stream));
-    DG_CUDA(dg_launch_queue_raster(job, c->nsm, c->stream));
-    if (c->timing) DG_CUDA(cudaEventRecord(c->ev[3], c->stream));
-    DG_CUDA(dg_launch_resolve(job, c->stream));
-    if (c->timing) {
-        DG_CUDA(cudaEventRecord(c->ev[4], c->stream));
-        c->ev_valid = true;
+    DG_CUDA(cudaMemsetAsync(S.d_counters, 0, 3 * sizeof(unsigned long long), S.stream));
+    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[0], S.stream));
+    DG_CUDA(dg_launch_vertex(job, S.stream));
+    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[1], S.stream));
+    DG_CUDA(dg_launch_setup_raster(job, c->nsm, S.stream));
+    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[2], S.stream));
+    DG_CUDA(dg_launch_queue_raster(job, c->nsm, S.stream));
+    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[3], S.stream));
+    DG_CUDA(dg_launch_resolve(job, S.stream));
+    if (S.timing) {
+        DG_CUDA(cudaEventRecord(S.ev[4], S.stream));
+        S.ev_valid = true;
     }
     return DG_OK;
 }
 
-}  // namespace
+}  // namespace dgh
 
 // Camera::new followed by the per-frame host setup of Scene::render, for callers
 // that hold no dg_ctx; uses only stack storage.
@@ -614,17 +618,11 @@ dg_status dg_ctx_create(int32_t device, dg_ctx** out) {
     DG_CUDA(cudaSetDevice(device));
     DG_CUDA(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
     DG_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
-    c->stream = c->own_stream;
-    for (int i = 0; i < dg_ctx::kSlots; i++) DG_CUDA(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming));
-    for (int i = 0; i < 5; i++) DG_CUDA(cudaEventCreate(&c->ev[i]));
-    dg_status e = dalloc(&c->d_counters, 4);
+    dg_status e = slot_init(c.get(), c->main, c->own_stream);
     if (e) return e;
-    e = dalloc(&c->d_err, 1);
-    if (e) return e;
-    DG_CUDA(cudaMemset(c->d_err, 0, 4));
     TexMap white;
     const uint8_t px[3] = {255, 255, 255};  // TextureMap::default, scene/mod.rs:128-135
-    e = tex_upload(c.get(), px, 3, 1, 1, 3, white);
+    e = tex_upload(px, 3, 1, 1, 3, white);
     if (e) return e;
     c->tex.push_back(white);
     *out = c.release();
@@ -638,7 +636,7 @@ dg_status dg_ctx_destroy(dg_ctx* c) {
         return DG_OK;
     }
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
+    cudaDeviceSynchronize();
     for (auto& t : c->tex) dfree(t.d_words);
     for (auto& o : c->objects) {
         dfree(o.d_pos); dfree(o.d_nrm); dfree(o.d_uv);
@@ -647,15 +645,8 @@ dg_status dg_ctx_destroy(dg_ctx* c) {
     for (auto& v : c->canvases) {
         dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
     }
-    dfree(c->d_tex); dfree(c->d_vrec); dfree(c->d_vshade); dfree(c->d_vmark); dfree(c->d_queue); dfree(c->d_queue_base);
-    dfree(c->d_counters); dfree(c->d_err);
-    for (int i = 0; i < dg_ctx::kSlots; i++) {
-        if (c->h_stage[i]) cudaFreeHost(c->h_stage[i]);
-        dfree(c->d_stage[i]);
-        if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
-    }
-    for (int i = 0; i < 5; i++)
-        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    dfree(c->d_tex);
+    slot_free(c->main);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return DG_OK;
@@ -665,44 +656,45 @@ dg_status dg_ctx_synchronize(dg_ctx* c) {
     if (!c) return DG_E_INVALID;
     dg_status e = set_device(c);
     if (e) return e;
-    DG_CUDA(cudaStreamSynchronize(c->stream));
-    return take_errors(c);
+    DG_CUDA(cudaStreamSynchronize(c->main.stream));
+    return slot_take_errors(c->main);
 }
 
 dg_status dg_ctx_set_stream(dg_ctx* c, void* stream) {
     if (!c) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;
-    DG_CUDA(cudaStreamSynchronize(c->stream));
-    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    DG_CUDA(cudaStreamSynchronize(c->main.stream));
+    c->main.stream = stream ? (cudaStream_t)stream : c->own_stream;
     return DG_OK;
 }
 
-void* dg_ctx_stream(dg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+void* dg_ctx_stream(dg_ctx* c) { return c ? (void*)c->main.stream : nullptr; }
 
 dg_status dg_ctx_set_timing(dg_ctx* c, int32_t enable) {
     if (!c) return DG_E_INVALID;
-    c->timing = enable != 0;
-    c->ev_valid = false;
+    c->main.timing = enable != 0;
+    c->main.ev_valid = false;
     return DG_OK;
 }
 
 dg_status dg_ctx_kernel_times(dg_ctx* c, float* ms, int32_t n) {
     if (!c || !ms || n < 0) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;
-    if (!c->ev_valid) return DG_E_INVALID;
-    DG_CUDA(cudaEventSynchronize(c->ev[4]));
-    for (int i = 0; i < n && i < 4; i++) DG_CUDA(cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]));
+    if (!c->main.ev_valid) return DG_E_INVALID;
+    DG_CUDA(cudaEventSynchronize(c->main.ev[4]));
+    for (int i = 0; i < n && i < 4; i++) DG_CUDA(cudaEventElapsedTime(&ms[i], c->main.ev[i], c->main.ev[i + 1]));
     return DG_OK;
 }
 
 dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
     if (!c || !out || n < 0) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;
-    DG_CUDA(cudaStreamSynchronize(c->stream));
+    JobSlot& S = c->main;
+    DG_CUDA(cudaStreamSynchronize(S.stream));
     unsigned long long h[3];
-    DG_CUDA(cudaMemcpy(h, c->d_counters, sizeof(h), cudaMemcpyDeviceToHost));
-    uint64_t v[8] = {c->last_vtx, c->last_tri, h[0] >> DG_PACK_SHIFT, h[0] & ((1ull << DG_PACK_SHIFT) - 1ull),
-                     h[1], h[2], c->last_h2d, c->last_launches};
+    DG_CUDA(cudaMemcpy(h, S.d_counters, sizeof(h), cudaMemcpyDeviceToHost));
+    uint64_t v[8] = {S.last_vtx, S.last_tri, h[0] >> DG_PACK_SHIFT, h[0] & ((1ull << DG_PACK_SHIFT) - 1ull),
+                     h[1], h[2], S.last_h2d, S.last_launches};
     for (int i = 0; i < n && i < 8; i++) out[i] = v[i];
     return DG_OK;
 }
@@ -716,7 +708,7 @@ dg_status dg_texmap_create(dg_ctx* c, const uint8_t* img, uint64_t len, uint64_t
     dg_status e = set_device(c);
     if (e) return e;
     TexMap t;
-    e = tex_upload(c, img, len, (uint32_t)w, (uint32_t)h, (uint32_t)comps, t);
+    e = tex_upload(img, len, (uint32_t)w, (uint32_t)h, (uint32_t)comps, t);
     if (e) return e;
     c->tex.push_back(t);
     c->tex_dirty = true;
@@ -817,7 +809,7 @@ dg_status dg_object_destroy(dg_ctx* c, int32_t id) {
         for (int32_t x : s.objects)
             if (x == id) return DG_E_INVALID;  // still referenced by a scene
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
+    cudaDeviceSynchronize();
     dfree(o->d_pos); dfree(o->d_nrm); dfree(o->d_uv);
     dfree(o->d_tri_pos); dfree(o->d_tri_uv); dfree(o->d_tri_nrm); dfree(o->d_mats);
     o->alive = false;
@@ -859,39 +851,7 @@ dg_status dg_scene_set_camera(dg_ctx* c, int32_t scene, const float pos[3], cons
 dg_status dg_scene_camera_op(dg_ctx* c, int32_t scene, int32_t op, const float* a) {
     Scene* s = get_scene(c, scene);
     if (!s || !a) return DG_E_INVALID;
-    Camera& cam = s->cam;
-    switch (op) {
-        case 0: cam.position = hadd(cam.position, hmul(cam.up, a[0])); break;     // move_up
-        case 1: cam.position = hadd(cam.position, hmul(cam.up, -a[0])); break;    // move_down
-        case 2: cam.position = hadd(cam.position, hmul(cam.u, -a[0])); break;     // move_left
-        case 3: cam.position = hadd(cam.position, hmul(cam.u, a[0])); break;      // move_right
-        case 4: cam.position = hadd(cam.position, hmul(hnormalized(hcross(cam.up, cam.u)), a[0])); break;
-        case 5: cam.position = hadd(cam.position, hmul(hnormalized(hcross(cam.u, cam.up)), a[0])); break;
-        case 6: {  // rotate_origin: Matrix4::rotate_y(theta.to_radians()) * v.as_vec4()
-            float th = a[0] * kRadsPerDeg;
-            float sn = std::sin(th), cs = std::cos(th);
-            HM4 r = hm_zero();
-            r.m[0][0] = cs; r.m[0][2] = sn; r.m[1][1] = 1.0f; r.m[2][0] = -sn; r.m[2][2] = cs; r.m[3][3] = 1.0f;
-            float p[4] = {cam.position.x, cam.position.y, cam.position.z, 1.0f}, po[4];
-            float d[4] = {cam.direction.x, cam.direction.y, cam.direction.z, 1.0f}, dout[4];
-            hm_vec(r, p, po);
-            hm_vec(r, d, dout);
-            cam.position = h3(po[0], po[1], po[2]);
-            cam.direction = h3(dout[0], dout[1], dout[2]);
-            break;
-        }
-        case 7: cam.position = h3(a[0], a[1], a[2]); break;
-        case 8: {  // Scene::move_camera_direction
-            int32_t dx = (int32_t)a[0], dy = (int32_t)a[1];
-            if (!((int64_t)dx < (int64_t)s->width) || !((int64_t)dy < (int64_t)s->height)) return DG_E_INVALID;
-            float fx = (float)dx / (float)s->width, fy = (float)dy / (float)s->height;
-            cam.direction = hnormalized(hadd(hadd(cam.direction, hmul(cam.u, fx)), hmul(cam.v, fy)));
-            camera_update_basis(cam);
-            break;
-        }
-        default: return DG_E_INVALID;
-    }
-    return DG_OK;
+    return camera_op(*s, op, a);
 }
 
 dg_status dg_scene_get_camera(dg_ctx* c, int32_t scene, float pos[3], float dir[3]) {
@@ -955,8 +915,8 @@ dg_status dg_canvas_create(dg_ctx* c, uint64_t width, uint64_t height, int32_t* 
     v.w = width;
     v.h = height;
     // Canvas::new: black frame (canvas.rs:368), no depth buffer yet
-    DG_CUDA(dg_launch_fill(v.d_colour, v.d_depth, n, 0xFF000000u, 0.0f, 1, 0, c->stream));
-    DG_CUDA(dg_launch_vis_reset(v.d_vis, n, c->stream));
+    DG_CUDA(dg_launch_fill(v.d_colour, v.d_depth, n, 0xFF000000u, 0.0f, 1, 0, c->main.stream));
+    DG_CUDA(dg_launch_vis_reset(v.d_vis, n, c->main.stream));
     v.alive = true;
     c->canvases.push_back(v);
     *out_id = (int32_t)c->canvases.size() - 1;
@@ -967,7 +927,7 @@ dg_status dg_canvas_destroy(dg_ctx* c, int32_t id) {
     Canvas* v = get_canvas(c, id);
     if (!v) return DG_E_INVALID;
     cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->main.stream);
     dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis);
     v->alive = false;
     return DG_OK;
@@ -980,7 +940,7 @@ dg_status dg_canvas_init_depth(dg_ctx* c, int32_t id, float depth) {
     if (e) return e;
     v->depth_max = depth;
     v->depth_init = true;
-    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, v->w * v->h, 0u, depth, 0, 1, c->stream));
+    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, v->w * v->h, 0u, depth, 0, 1, c->main.stream));
     return DG_OK;
 }
 
@@ -998,6 +958,7 @@ dg_status dg_canvas_resize(dg_ctx* c, int32_t id, uint64_t width, uint64_t heigh
     if (width > 65535 || height > 65535) return DG_E_LIMIT;
     dg_status e = set_device(c);
     if (e) return e;
+    cudaStream_t st = c->main.stream;
     uint64_t n_old = v->w * v->h, n = width * height;
     // Vec::resize keeps the first min(old, new) pixels and pads with black (canvas.rs:390)
     uint32_t* col = nullptr;
@@ -1007,10 +968,10 @@ dg_status dg_canvas_resize(dg_ctx* c, int32_t id, uint64_t width, uint64_t heigh
         dfree(col); dfree(dep); dfree(vis);
         return e;
     }
-    DG_CUDA(dg_launch_fill(col, dep, n, 0xFF000000u, 0.0f, 1, 0, c->stream));
-    DG_CUDA(cudaMemcpyAsync(col, v->d_colour, std::min(n, n_old) * 4, cudaMemcpyDeviceToDevice, c->stream));
-    DG_CUDA(dg_launch_vis_reset(vis, n, c->stream));
-    DG_CUDA(cudaStreamSynchronize(c->stream));
+    DG_CUDA(dg_launch_fill(col, dep, n, 0xFF000000u, 0.0f, 1, 0, st));
+    DG_CUDA(cudaMemcpyAsync(col, v->d_colour, std::min(n, n_old) * 4, cudaMemcpyDeviceToDevice, st));
+    DG_CUDA(dg_launch_vis_reset(vis, n, st));
+    DG_CUDA(cudaStreamSynchronize(st));
     dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis);
     v->d_colour = col;
     v->d_depth = dep;
@@ -1019,7 +980,7 @@ dg_status dg_canvas_resize(dg_ctx* c, int32_t id, uint64_t width, uint64_t heigh
     v->h = height;
     // init_depth(depth_max) (canvas.rs:392)
     v->depth_init = true;
-    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, n, 0u, v->depth_max, 0, 1, c->stream));
+    DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, n, 0u, v->depth_max, 0, 1, st));
     return DG_OK;
 }
 
@@ -1029,7 +990,7 @@ dg_status dg_canvas_clear(dg_ctx* c, int32_t id) {
     dg_status e = set_device(c);
     if (e) return e;
     DG_CUDA(dg_launch_fill(v->d_colour, v->d_depth, v->w * v->h, 0xFF9BBAFFu, v->depth_max, 1, v->depth_init ? 1 : 0,
-                           c->stream));
+                           c->main.stream));
     return DG_OK;
 }
 
@@ -1040,10 +1001,11 @@ dg_status dg_canvas_read(dg_ctx* c, int32_t id, uint8_t* bgra, float* depth) {
     dg_status e = set_device(c);
     if (e) return e;
     uint64_t n = v->w * v->h;
-    if (bgra) DG_CUDA(cudaMemcpyAsync(bgra, v->d_colour, n * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (depth) DG_CUDA(cudaMemcpyAsync(depth, v->d_depth, n * 4, cudaMemcpyDeviceToHost, c->stream));
-    DG_CUDA(cudaStreamSynchronize(c->stream));
-    return take_errors(c);
+    cudaStream_t st = c->main.stream;
+    if (bgra) DG_CUDA(cudaMemcpyAsync(bgra, v->d_colour, n * 4, cudaMemcpyDeviceToHost, st));
+    if (depth) DG_CUDA(cudaMemcpyAsync(depth, v->d_depth, n * 4, cudaMemcpyDeviceToHost, st));
+    DG_CUDA(cudaStreamSynchronize(st));
+    return slot_take_errors(c->main);
 }
 
 dg_status dg_canvas_write(dg_ctx* c, int32_t id, const uint8_t* bgra, const float* depth) {
@@ -1053,9 +1015,10 @@ dg_status dg_canvas_write(dg_ctx* c, int32_t id, const uint8_t* bgra, const floa
     dg_status e = set_device(c);
     if (e) return e;
     uint64_t n = v->w * v->h;
-    if (bgra) DG_CUDA(cudaMemcpyAsync(v->d_colour, bgra, n * 4, cudaMemcpyHostToDevice, c->stream));
-    if (depth) DG_CUDA(cudaMemcpyAsync(v->d_depth, depth, n * 4, cudaMemcpyHostToDevice, c->stream));
-    DG_CUDA(cudaStreamSynchronize(c->stream));
+    cudaStream_t st = c->main.stream;
+    if (bgra) DG_CUDA(cudaMemcpyAsync(v->d_colour, bgra, n * 4, cudaMemcpyHostToDevice, st));
+    if (depth) DG_CUDA(cudaMemcpyAsync(v->d_depth, depth, n * 4, cudaMemcpyHostToDevice, st));
+    DG_CUDA(cudaStreamSynchronize(st));
     return DG_OK;
 }
 

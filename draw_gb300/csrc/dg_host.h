@@ -1,0 +1,164 @@
+// dg_host.h -- host-side state of the GB300 rasterizer, shared by the C ABI
+// (dg_api.cu) and the render server (dg_server.cu): scene and camera state,
+// resident resources, the per-frame host setup of Scene::render and the
+// launch of one render job on a job slot.
+//
+// Host floating point follows the reference's Rust semantics: the files
+// including this header are compiled with -ffp-contract=off, so every
+// expression rounds each operation to f32 in source order.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dg_internal.cuh"
+
+namespace dgh {
+
+// ------------------------------------------------------------ host vectors
+struct HV3 {
+    float x, y, z;
+};
+inline HV3 h3(float x, float y, float z) { return HV3{x, y, z}; }
+inline HV3 hadd(HV3 a, HV3 b) { return h3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline HV3 hsub(HV3 a, HV3 b) { return h3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline HV3 hmul(HV3 a, float s) { return h3(a.x * s, a.y * s, a.z * s); }
+inline HV3 hdiv(HV3 a, float s) { return h3(a.x / s, a.y / s, a.z / s); }
+inline float hdot(HV3 a, HV3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }       // linalg.rs:182-184
+inline float hnorm(HV3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }  // linalg.rs:167-171
+inline HV3 hnormalized(HV3 a) { return hdiv(a, hnorm(a)); }                           // linalg.rs:173-175
+inline HV3 hcross(HV3 a, HV3 b) {                                                      // linalg.rs:186-200
+    return h3((a.y * b.z) - (a.z * b.y), (a.z * b.x) - (a.x * b.z), (a.x * b.y) - (a.y * b.x));
+}
+
+struct HM4 {
+    float m[4][4];
+};
+
+struct Camera {  // scene/mod.rs:282-294
+    HV3 position, direction, up;
+    float top, bottom, right, left;
+    float near_, far_;
+    HV3 u, v, w;
+};
+
+struct Scene {  // scene/mod.rs:749-757
+    uint64_t width = 0, height = 0;
+    Camera cam;
+    std::vector<int32_t> objects;
+    std::vector<HV3> lights;
+    int32_t exponent = 2;
+};
+
+dg_status camera_init(Camera& c, HV3 pos, HV3 dir, float ratio, float near_, float far_, float fov_x);
+void camera_update_basis(Camera& c);
+dg_status camera_op(Scene& s, int32_t op, const float* a);
+// gen_transformation_matrix (scene/mod.rs:817-899) and gen_view_planes (:481-593).
+dg_status frame_setup(Scene& s, float M[4][4], float planes[6][4]);
+
+// ------------------------------------------------------------- resources
+struct TexMap {
+    uint32_t* d_words = nullptr;
+    uint64_t len = 0;
+    uint32_t w = 0, h = 0, comps = 0;
+};
+
+struct Object {
+    bool alive = false;
+    float4* d_pos = nullptr;
+    float4* d_nrm = nullptr;
+    float2* d_uv = nullptr;
+    uint4* d_tri_pos = nullptr;
+    uint4* d_tri_uv = nullptr;
+    uint4* d_tri_nrm = nullptr;
+    DgMatDev* d_mats = nullptr;
+    uint32_t nv = 0, nn = 0, nuv = 0, ntri_opaque = 0, nmats = 0;
+    std::vector<float> h_pos;                        // for the transparent pass sort
+    std::vector<std::vector<uint32_t>> transparent;  // 9 indices per triangle, current order
+    std::vector<int32_t> transparent_mat;
+};
+
+struct Canvas {
+    bool alive = false;
+    uint64_t w = 0, h = 0;
+    uint32_t* d_colour = nullptr;
+    float* d_depth = nullptr;
+    uint64_t* d_vis = nullptr;
+    bool depth_init = false;
+    float depth_max = 0.0f;
+    float off_x = 0.0f, off_y = 0.0f;
+};
+
+// The buffers one frame renders into.
+struct FrameTarget {
+    uint32_t* colour;
+    float* depth;
+    uint64_t* vis;  // all DG_VIS_EMPTY on entry; left so on exit
+    uint64_t w, h;
+    float clear_depth;
+    float off_x, off_y;
+};
+
+// Scratch, staging and stream of one render job in flight. The context owns
+// one; the render server owns one per concurrent batch.
+struct JobSlot {
+    cudaStream_t stream = nullptr;
+    float4* d_vrec = nullptr;
+    size_t vrec_cap = 0;
+    float4* d_vshade = nullptr;
+    size_t vshade_cap = 0;
+    uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
+    size_t vmark_cap = 0;
+    DgQueueRec* d_queue = nullptr;
+    uint32_t* d_queue_base = nullptr;
+    size_t queue_cap = 0;
+    size_t queue_base_cap = 0;
+    uint32_t small_max_px = DG_SMALL_MAX_PX;
+    unsigned long long* d_counters = nullptr;  // [0] queue counter, [1] covered px, [2] overflow
+    uint32_t* d_err = nullptr;
+    static const int kStage = 4;  // pinned staging ring for job descriptors
+    void* h_stage[kStage] = {};
+    void* d_stage[kStage] = {};
+    size_t stage_cap[kStage] = {};
+    cudaEvent_t stage_ev[kStage] = {};
+    int stage = 0;
+    bool timing = false;
+    cudaEvent_t ev[5] = {};
+    bool ev_valid = false;
+    uint64_t last_vtx = 0, last_tri = 0, last_h2d = 0, last_launches = 0;
+    uint64_t scratch_bytes = 0;  // device bytes held by the scratch buffers
+};
+
+}  // namespace dgh
+
+struct dg_ctx {
+    int device = 0;
+    int nsm = 152;
+    cudaStream_t own_stream = nullptr;
+    std::vector<dgh::TexMap> tex;  // [0] = 1x1 white default map
+    DgTexDev* d_tex = nullptr;
+    size_t d_tex_cap = 0;
+    bool tex_dirty = true;
+    std::vector<dgh::Object> objects;
+    std::vector<dgh::Scene> scenes;
+    std::vector<dgh::Canvas> canvases;
+    dgh::JobSlot main;  // the slot of dg_scene_render / dg_render_batch (main.stream = the context stream)
+};
+
+namespace dgh {
+
+dg_status set_device(dg_ctx* c);
+dg_status slot_init(dg_ctx* c, JobSlot& s, cudaStream_t stream);
+void slot_free(JobSlot& s);
+// Returns the lowest error code the slot's kernels raised since the last call, and clears it.
+dg_status slot_take_errors(JobSlot& s);
+// Uploads the texture table if textures were added.
+dg_status sync_tex_table(dg_ctx* c, cudaStream_t s);
+// Device bytes slot s's scratch will hold after launching a job of V vertices,
+// T triangles and L lights per vertex (same sizing rules as launch_frames).
+uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L);
+// Builds and launches one render job over n frames on slot s (asynchronous).
+dg_status launch_frames(dg_ctx* c, JobSlot& s, Scene* const* scenes, const FrameTarget* targets, uint32_t n);
+
+}  // namespace dgh

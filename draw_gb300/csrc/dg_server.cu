@@ -1,0 +1,417 @@
+// dg_server.cu -- a continuous-batching render server on one GPU.
+//
+// Clients submit render requests (a resident object, a frame size, a camera,
+// lights) from any thread. A scheduler thread admits pending requests in
+// arrival order while the device-memory budget allows (each request holds its
+// own colour, depth and visibility buffers; job-slot scratch counts too),
+// packs up to max_batch of them into one render job, and launches it on a free
+// job slot (its own stream and scratch). Several batches are in flight at
+// once, so requests that arrive while others run are admitted as soon as a
+// slot and memory free up, and their work overlaps on the device. A host
+// callback on the slot's stream stamps each request's completion time.
+//
+// Every request renders exactly as dg_scene_render would render it alone: a
+// batch is the same kernels over more frames, with per-frame keys and buffers.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "dg_host.h"
+
+using namespace dgh;
+
+namespace {
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+enum ReqState { kPending = 0, kRunning = 1, kDone = 2 };
+
+struct Request {
+    uint64_t ticket = 0;
+    Scene scene;
+    FrameTarget tgt{};
+    void* mem = nullptr;  // one allocation: colour | depth | vis
+    uint64_t bytes = 0;
+    double t_submit = 0, t_start = 0, t_done = 0;
+    int state = kPending;
+    dg_status status = DG_OK;
+    bool discard = false;
+};
+
+struct Slot {
+    JobSlot js;
+    bool busy = false;
+    std::vector<Request*> batch;
+    uint32_t* h_err = nullptr;  // pinned copy of the slot's error word
+    struct dg_server* srv = nullptr;
+};
+
+}  // namespace
+
+struct dg_server {
+    dg_ctx* ctx = nullptr;
+    uint64_t budget = 0;
+    uint64_t used = 0;       // request buffers + slot scratch
+    uint64_t peak_used = 0;
+    uint64_t held_done = 0;  // buffers of finished requests not yet collected by dg_server_wait
+    uint32_t max_batch = 1;
+    std::vector<std::unique_ptr<Slot>> slots;
+    std::deque<Request*> pending;
+    std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
+    std::vector<void*> to_free;  // buffers of finished discard requests, freed by the scheduler
+    std::vector<uint64_t> to_free_bytes;
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done;
+    std::thread thr;
+    bool stop = false;
+    uint64_t next_ticket = 1;
+    std::vector<double> latencies_ms;
+    uint64_t batches = 0, frames = 0;
+    dg_status sticky = DG_OK;  // first launch error, reported by later calls
+    cudaStream_t copy_stream = nullptr;
+};
+
+namespace {
+
+uint64_t request_bytes(uint64_t w, uint64_t h) { return w * h * (4 + 4 + 8); }
+
+// Host callback at the end of a batch on its slot stream (no CUDA calls allowed here).
+void CUDART_CB batch_done(void* arg) {
+    Slot* sl = static_cast<Slot*>(arg);
+    dg_server* s = sl->srv;
+    const double t = now_s();
+    std::lock_guard<std::mutex> lk(s->mu);
+    dg_status st = DG_OK;
+    for (int b = 1; b < 32; b++)
+        if (*sl->h_err & (1u << b)) {
+            st = (dg_status)b;
+            break;
+        }
+    for (Request* r : sl->batch) {
+        r->t_done = t;
+        r->state = kDone;
+        r->status = st;
+        s->latencies_ms.push_back((r->t_done - r->t_submit) * 1e3);
+        if (r->discard) {
+            s->to_free.push_back(r->mem);
+            s->to_free_bytes.push_back(r->bytes);
+            r->mem = nullptr;
+        } else {
+            s->held_done += r->bytes;  // kept until the client collects the frame
+        }
+    }
+    s->frames += sl->batch.size();
+    sl->batch.clear();
+    sl->busy = false;
+    s->cv_sched.notify_all();
+    s->cv_done.notify_all();
+}
+
+// Launches one batch on slot sl (called by the scheduler without the lock held).
+dg_status launch_batch(dg_server* s, Slot* sl, std::vector<Request*>& batch, uint64_t reserved) {
+    cudaStream_t st = sl->js.stream;
+    const uint64_t scratch_before = sl->js.scratch_bytes;
+    // the admission reserved the predicted scratch growth; settle it against the actual one
+    auto settle = [&]() {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->used = s->used - reserved + (sl->js.scratch_bytes - scratch_before);
+        s->peak_used = std::max(s->peak_used, s->used);
+    };
+    for (Request* r : batch) {
+        const uint64_t n = r->scene.width * r->scene.height;
+        if (cudaMallocAsync(&r->mem, r->bytes, st) != cudaSuccess) {
+            cudaGetLastError();
+            r->mem = nullptr;
+            settle();
+            return DG_E_OOM;
+        }
+        uint8_t* base = static_cast<uint8_t*>(r->mem);
+        r->tgt.vis = reinterpret_cast<uint64_t*>(base);
+        r->tgt.colour = reinterpret_cast<uint32_t*>(base + n * 8);
+        r->tgt.depth = reinterpret_cast<float*>(base + n * 12);
+        r->tgt.w = r->scene.width;
+        r->tgt.h = r->scene.height;
+        r->tgt.off_x = r->tgt.off_y = 0.0f;
+        if (cudaMemsetAsync(r->tgt.vis, 0xFF, n * 8, st) != cudaSuccess) {
+            settle();
+            return DG_E_CUDA;
+        }
+    }
+    std::vector<Scene*> sc(batch.size());
+    std::vector<FrameTarget> tg(batch.size());
+    for (size_t i = 0; i < batch.size(); i++) {
+        sc[i] = &batch[i]->scene;
+        tg[i] = batch[i]->tgt;
+    }
+    dg_status e = launch_frames(s->ctx, sl->js, sc.data(), tg.data(), (uint32_t)batch.size());
+    settle();
+    if (e) return e;
+    if (cudaMemcpyAsync(sl->h_err, sl->js.d_err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess) return DG_E_CUDA;
+    if (cudaMemsetAsync(sl->js.d_err, 0, 4, st) != cudaSuccess) return DG_E_CUDA;
+    sl->batch = batch;
+    if (cudaLaunchHostFunc(st, batch_done, sl) != cudaSuccess) return DG_E_CUDA;
+    return DG_OK;
+}
+
+void scheduler(dg_server* s) {
+    cudaSetDevice(s->ctx->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        // release the buffers of finished discard requests
+        if (!s->to_free.empty()) {
+            std::vector<void*> fr;
+            fr.swap(s->to_free);
+            uint64_t b = 0;
+            for (uint64_t x : s->to_free_bytes) b += x;
+            s->to_free_bytes.clear();
+            lk.unlock();
+            for (void* p : fr) cudaFreeAsync(p, s->copy_stream);
+            lk.lock();
+            s->used -= b;
+        }
+        Slot* free_slot = nullptr;
+        bool any_busy = false;
+        for (auto& sl : s->slots) {
+            if (sl->busy)
+                any_busy = true;
+            else if (!free_slot)
+                free_slot = sl.get();
+        }
+        if (s->stop && s->pending.empty() && !any_busy) break;
+        std::vector<Request*> batch;
+        uint64_t reserved = 0;  // growth of the slot's scratch this batch will cause
+        if (free_slot && !s->pending.empty()) {
+            // admit in arrival order while the batch size and the memory budget allow; the
+            // budget covers the requests' buffers and the scratch growth of the batch
+            uint64_t V = 0, T = 0;
+            uint32_t L = 1;
+            const uint64_t cur = free_slot->js.scratch_bytes;
+            while (!s->pending.empty() && batch.size() < s->max_batch) {
+                Request* r = s->pending.front();
+                const Object& o = s->ctx->objects[r->scene.objects[0]];
+                const uint64_t V2 = V + o.nv, T2 = T + o.ntri_opaque;
+                const uint32_t L2 = std::max<uint32_t>(L, (uint32_t)r->scene.lights.size());
+                const uint64_t after = slot_scratch_after(free_slot->js, V2, T2, L2);
+                const uint64_t grow_by = after > cur ? after - cur : 0;
+                if (s->used + r->bytes + (grow_by - reserved) > s->budget) break;
+                s->used += r->bytes + (grow_by - reserved);
+                reserved = grow_by;
+                V = V2;
+                T = T2;
+                L = L2;
+                s->peak_used = std::max(s->peak_used, s->used);
+                s->pending.pop_front();
+                r->state = kRunning;
+                r->t_start = now_s();
+                batch.push_back(r);
+            }
+        }
+        if (batch.empty()) {
+            if (free_slot && !any_busy && !s->pending.empty() && s->held_done == 0 && s->to_free.empty()) {
+                // nothing runs and nothing waits to be collected, yet the head request
+                // (with the scratch its job needs) does not fit the budget: refuse it
+                Request* r = s->pending.front();
+                s->pending.pop_front();
+                r->state = kDone;
+                r->status = DG_E_OOM;
+                r->t_done = now_s();
+                s->cv_done.notify_all();
+                continue;
+            }
+            s->cv_sched.wait(lk);
+            continue;
+        }
+        free_slot->busy = true;
+        s->batches++;
+        lk.unlock();
+        dg_status e = launch_batch(s, free_slot, batch, reserved);
+        lk.lock();
+        if (e) {
+            // the batch did not launch: its requests complete with the error
+            if (!s->sticky) s->sticky = e;
+            const double t = now_s();
+            for (Request* r : batch) {
+                r->state = kDone;
+                r->status = e;
+                r->t_done = t;
+                if (r->mem) {
+                    s->to_free.push_back(r->mem);
+                    s->to_free_bytes.push_back(r->bytes);
+                    r->mem = nullptr;
+                } else {
+                    s->used -= r->bytes;
+                }
+            }
+            free_slot->batch.clear();
+            free_slot->busy = false;
+            s->cv_done.notify_all();
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+dg_status dg_server_create(dg_ctx* ctx, uint64_t budget_bytes, uint32_t max_batch, uint32_t streams,
+                           dg_server** out) {
+    if (!ctx || !out || max_batch == 0 || streams == 0 || streams > 16) return DG_E_INVALID;
+    *out = nullptr;
+    dg_status e = set_device(ctx);
+    if (e) return e;
+    std::unique_ptr<dg_server> s(new (std::nothrow) dg_server());
+    if (!s) return DG_E_OOM;
+    s->ctx = ctx;
+    s->budget = budget_bytes;
+    s->max_batch = max_batch;
+    // keep freed request buffers in the stream-ordered pool for reuse
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+        uint64_t thr = budget_bytes;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    cudaGetLastError();
+    if (cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return DG_E_CUDA;
+    e = sync_tex_table(ctx, ctx->main.stream);
+    if (e) return e;
+    for (uint32_t i = 0; i < streams; i++) {
+        auto sl = std::make_unique<Slot>();
+        sl->srv = s.get();
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return DG_E_CUDA;
+        e = slot_init(ctx, sl->js, st);
+        if (e) return e;
+        if (cudaMallocHost((void**)&sl->h_err, 4) != cudaSuccess) return DG_E_OOM;
+        *sl->h_err = 0;
+        s->slots.push_back(std::move(sl));
+    }
+    s->thr = std::thread(scheduler, s.get());
+    *out = s.release();
+    return DG_OK;
+}
+
+dg_status dg_server_submit(dg_server* s, const dg_request* q, uint64_t* ticket) {
+    if (!s || !q || !ticket) return DG_E_INVALID;
+    dg_ctx* c = s->ctx;
+    if (q->object < 0 || (size_t)q->object >= c->objects.size() || !c->objects[q->object].alive) return DG_E_INVALID;
+    if (!c->objects[q->object].transparent.empty()) return DG_E_LIMIT;
+    if (q->width == 0 || q->height == 0 || q->width > 65535 || q->height > 65535) return DG_E_INVALID;
+    if (q->nlights == 0 || q->nlights > DG_MAX_LIGHTS) return DG_E_INVALID;
+    auto r = std::make_unique<Request>();
+    r->scene.width = q->width;
+    r->scene.height = q->height;
+    r->scene.objects.push_back(q->object);
+    for (uint32_t l = 0; l < q->nlights; l++) r->scene.lights.push_back(h3(q->lights[l][0], q->lights[l][1], q->lights[l][2]));
+    r->scene.exponent = q->exponent;
+    const float ratio = (float)q->width / (float)q->height;
+    dg_status e = camera_init(r->scene.cam, h3(q->cam_pos[0], q->cam_pos[1], q->cam_pos[2]),
+                              h3(q->cam_dir[0], q->cam_dir[1], q->cam_dir[2]), ratio, q->near_, q->far_, q->fov_x_deg);
+    if (e) return e;
+    r->tgt.clear_depth = q->clear_depth;
+    r->bytes = request_bytes(q->width, q->height);
+    r->discard = q->discard != 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return DG_E_INVALID;
+    if (r->bytes > s->budget) return DG_E_OOM;  // could never be admitted
+    r->ticket = s->next_ticket++;
+    r->t_submit = now_s();
+    *ticket = r->ticket;
+    s->pending.push_back(r.get());
+    s->reqs.emplace(r->ticket, std::move(r));
+    s->cv_sched.notify_all();
+    return DG_OK;
+}
+
+dg_status dg_server_wait(dg_server* s, uint64_t ticket, uint8_t* bgra, float* depth, double* latency_ms) {
+    if (!s) return DG_E_INVALID;
+    Request* r = nullptr;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return DG_E_INVALID;
+    r = it->second.get();
+    s->cv_done.wait(lk, [&] { return r->state == kDone; });
+    dg_status st = r->status;
+    if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
+    void* mem = r->mem;
+    const uint64_t bytes = r->bytes;
+    const uint64_t n = r->scene.width * r->scene.height;
+    r->mem = nullptr;
+    s->reqs.erase(it);
+    lk.unlock();
+    if (mem) {
+        cudaSetDevice(s->ctx->device);
+        uint8_t* base = static_cast<uint8_t*>(mem);
+        if (st == DG_OK && bgra && cudaMemcpy(bgra, base + n * 8, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = DG_E_CUDA;
+        if (st == DG_OK && depth && cudaMemcpy(depth, base + n * 12, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = DG_E_CUDA;
+        lk.lock();
+        s->to_free.push_back(mem);
+        s->to_free_bytes.push_back(bytes);
+        s->held_done -= bytes;
+        s->cv_sched.notify_all();
+    }
+    return st;
+}
+
+dg_status dg_server_stats(dg_server* s, double* out, int32_t n) {
+    if (!s || !out || n < 0) return DG_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    std::vector<double> l = s->latencies_ms;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double p) {
+        if (l.empty()) return 0.0;
+        size_t i = (size_t)std::min<double>(l.size() - 1, std::max(0.0, p * (l.size() - 1) + 0.5));
+        return l[i];
+    };
+    double v[8] = {(double)l.size(), pct(0.5), pct(0.99), l.empty() ? 0.0 : l.back(), (double)s->batches,
+                   s->batches ? (double)s->frames / (double)s->batches : 0.0, (double)s->peak_used,
+                   (double)s->sticky};
+    for (int i = 0; i < n && i < 8; i++) out[i] = v[i];
+    return DG_OK;
+}
+
+dg_status dg_server_reset_stats(dg_server* s) {
+    if (!s) return DG_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->latencies_ms.clear();
+    s->batches = 0;
+    s->frames = 0;
+    s->peak_used = s->used;
+    return DG_OK;
+}
+
+dg_status dg_server_destroy(dg_server* s) {
+    if (!s) return DG_E_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv_sched.notify_all();
+    }
+    if (s->thr.joinable()) s->thr.join();
+    cudaSetDevice(s->ctx->device);
+    for (auto& kv : s->reqs)
+        if (kv.second->mem) cudaFreeAsync(kv.second->mem, s->copy_stream);
+    for (void* p : s->to_free) cudaFreeAsync(p, s->copy_stream);
+    cudaStreamSynchronize(s->copy_stream);
+    for (auto& sl : s->slots) {
+        cudaStream_t st = sl->js.stream;
+        slot_free(sl->js);
+        if (st) cudaStreamDestroy(st);
+        if (sl->h_err) cudaFreeHost(sl->h_err);
+    }
+    cudaStreamDestroy(s->copy_stream);
+    delete s;
+    return DG_OK;
+}
+
+}  // extern "C"

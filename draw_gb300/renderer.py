@@ -63,6 +63,12 @@ SIGNATURES = {
     "dg_scene_render": (_i32, [_P, _i32, _i32]),
     "dg_render_batch": (_i32, [_P, _P, _P, _u32]),
     "dg_render_noalloc": (_i32, [_P, _P, _P, _u32, _P, _u32, _P, _P, _P, _P]),
+    "dg_server_create": (_i32, [_P, _u64, _u32, _u32, _P]),
+    "dg_server_submit": (_i32, [_P, _P, _P]),
+    "dg_server_wait": (_i32, [_P, _u64, _P, _P, _P]),
+    "dg_server_stats": (_i32, [_P, _P, _i32]),
+    "dg_server_reset_stats": (_i32, [_P]),
+    "dg_server_destroy": (_i32, [_P]),
 }
 
 
@@ -79,6 +85,17 @@ class dg_material(ctypes.Structure):
 
 class dg_mesh_desc(ctypes.Structure):
     _fields_ = [("tris", ctypes.c_void_p), ("ntri", ctypes.c_uint64), ("texture_idx", ctypes.c_int32)]
+
+
+MAX_LIGHTS = 8
+
+
+class dg_request(ctypes.Structure):
+    _fields_ = [("object", ctypes.c_int32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("cam_pos", ctypes.c_float * 3), ("cam_dir", ctypes.c_float * 3), ("near_", ctypes.c_float),
+                ("far_", ctypes.c_float), ("fov_x_deg", ctypes.c_float), ("lights", (ctypes.c_float * 3) * MAX_LIGHTS),
+                ("nlights", ctypes.c_uint32), ("exponent", ctypes.c_int32), ("clear_depth", ctypes.c_float),
+                ("discard", ctypes.c_int32)]
 
 
 # dg_render_noalloc's argument structs (include/draw_gpu.h).
@@ -449,3 +466,69 @@ def build_scene(desc, ctx: Context | None = None) -> BuiltScene:
     canvas.init_depth(desc.clear_depth)
     canvas.apply_offset(*desc.offset)
     return BuiltScene(scene, canvas, objects, texmaps)
+
+
+def upload_object(o, texmaps: list, ctx: Context) -> Object:
+    """Uploads one scenes.ObjectDesc whose material maps index `texmaps`."""
+    mats = [Texture(f"m{i}", m.ka, m.kd, m.ks, m.alpha, texmaps[m.map_ka] if m.map_ka >= 0 else None,
+                    texmaps[m.map_kd] if m.map_kd >= 0 else None) for i, m in enumerate(o.materials)]
+    meshes = [IndexedMesh(f"mesh{i}", m.tris, m.texture_idx) for i, m in enumerate(o.meshes)]
+    return Object("object", o.vertices, o.normals, o.uvs, meshes, mats, ctx)
+
+
+class Server:
+    """The continuous-batching render server (dg_server_*): submit requests from
+    any thread, wait for each one, read latency percentiles."""
+
+    def __init__(self, ctx: Context, budget_bytes: int, max_batch: int = 64, streams: int = 3):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        _chk(ctx.lib.dg_server_create(ctx.h, int(budget_bytes), max_batch, streams, ctypes.byref(h)), "server")
+        self.h = h
+
+    @staticmethod
+    def request(obj: Object, width, height, cam_pos, cam_dir, near, far, fov_x, lights, exponent=2,
+                clear_depth=float("inf"), discard=False) -> dg_request:
+        r = dg_request()
+        r.object, r.width, r.height = obj.id, width, height
+        r.cam_pos[:] = [float(x) for x in cam_pos]
+        r.cam_dir[:] = [float(x) for x in cam_dir]
+        r.near_, r.far_, r.fov_x_deg = near, far, fov_x
+        lights = np.asarray(lights, np.float32).reshape(-1, 3)
+        for i, l in enumerate(lights):
+            r.lights[i][:] = [float(x) for x in l]
+        r.nlights, r.exponent, r.clear_depth, r.discard = len(lights), exponent, clear_depth, 1 if discard else 0
+        return r
+
+    def submit(self, req: dg_request) -> int:
+        t = ctypes.c_uint64()
+        _chk(self.ctx.lib.dg_server_submit(self.h, ctypes.byref(req), ctypes.byref(t)), "server submit")
+        return t.value
+
+    def wait(self, ticket: int, width: int = 0, height: int = 0, read: bool = False):
+        """Returns (bgra, depth, latency_ms); the frame only when read=True."""
+        lat = ctypes.c_double()
+        bgra = np.empty((height, width, 4), np.uint8) if read else None
+        depth = np.empty((height, width), np.float32) if read else None
+        _chk(self.ctx.lib.dg_server_wait(self.h, ticket, _ptr(bgra), _ptr(depth), ctypes.byref(lat)), "server wait")
+        return bgra, depth, lat.value
+
+    def stats(self) -> dict:
+        v = (ctypes.c_double * 8)()
+        _chk(self.ctx.lib.dg_server_stats(self.h, v, 8), "server stats")
+        keys = ["completed", "p50_ms", "p99_ms", "max_ms", "batches", "mean_batch", "peak_bytes", "error"]
+        return dict(zip(keys, list(v)))
+
+    def reset_stats(self):
+        _chk(self.ctx.lib.dg_server_reset_stats(self.h), "server reset_stats")
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.dg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

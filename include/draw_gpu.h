@@ -154,6 +154,47 @@ dg_status dg_scene_render(dg_ctx* ctx, int32_t scene, int32_t canvas);
  * stage (the batched form). Equivalent to n dg_scene_render calls. */
 dg_status dg_render_batch(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n);
 
+/* ------------------------------------------------------------ render server
+ * Serving form of the draw call. The reference renders one frame per call of
+ * Scene::render from its application loop (app/mod.rs:196); this server accepts
+ * render requests from any thread as they arrive, keeps meshes and textures
+ * resident (objects of the context), admits requests in arrival order against
+ * a device-memory budget (each request holds W*H*16 bytes of colour, depth and
+ * visibility buffers; job scratch counts too), packs up to max_batch admitted
+ * requests into one batched render job, and keeps up to `streams` jobs in flight
+ * on separate streams. Each request renders exactly as dg_scene_render would
+ * render it alone. While a server runs, its context must not be modified or
+ * used for other rendering. */
+typedef struct dg_server dg_server;
+
+typedef struct {
+    int32_t object;             /* object id from dg_object_create (opaque meshes only) */
+    uint32_t width, height;     /* frame size: Scene::new(width, height) and its canvas */
+    float cam_pos[3];
+    float cam_dir[3];
+    float near_, far_, fov_x_deg;
+    float lights[DG_MAX_LIGHTS][3];
+    uint32_t nlights;
+    int32_t exponent;
+    float clear_depth;          /* Canvas::init_depth value */
+    int32_t discard;            /* 1: free the frame at completion (only status and latency are kept) */
+} dg_request;
+
+dg_status dg_server_create(dg_ctx* ctx, uint64_t budget_bytes, uint32_t max_batch, uint32_t streams,
+                           dg_server** out);
+/* Thread-safe. DG_E_OOM if the request alone exceeds the budget. */
+dg_status dg_server_submit(dg_server* s, const dg_request* r, uint64_t* ticket);
+/* Blocks until the request is done; copies its frame (BGRA, row 0 = top) and
+ * depth to host memory when the pointers are not NULL, releases it, and
+ * returns its status. latency_ms = completion - submission. */
+dg_status dg_server_wait(dg_server* s, uint64_t ticket, uint8_t* bgra, float* depth, double* latency_ms);
+/* [0] completed requests, [1] p50 latency ms, [2] p99 ms, [3] max ms, [4] batches,
+ * [5] mean requests per batch, [6] peak device bytes held, [7] first launch error. */
+dg_status dg_server_stats(dg_server* s, double* out, int32_t n);
+dg_status dg_server_reset_stats(dg_server* s);
+/* Drains the pending requests, then frees the server. */
+dg_status dg_server_destroy(dg_server* s);
+
 /* ----------------------------------------------------- render without allocating
  * No counterpart in the reference: an extra entry point for callers that cannot
  * allocate device memory while they draw, for example a host application or

@@ -1,0 +1,116 @@
+"""The continuous-batching render server: every request served in a concurrent
+mix of sizes, meshes and cameras renders exactly as it renders alone through
+Scene::render (coverage and depth bit-exact, colour within COLOUR_TOL_LSB);
+admission respects the device-memory budget."""
+import math
+import threading
+
+import numpy as np
+import pytest
+
+from draw_gb300 import scenes as S
+from helpers import COLOUR_TOL_LSB, compare, describe
+
+pytestmark = pytest.mark.gpu
+
+
+def _pool():
+    """Three meshes, two textures, and a list of (object index, w, h, camera, light) requests."""
+    meshes = [S.mesh_for_tris("torus", 3000), S.mesh_for_tris("sphere", 8000), S.mesh_for_tris("torus", 20000)]
+    texs = [S.value_noise_checker(256, 256, 5), S.value_noise_checker(128, 128, 6, comps=3)]
+    objs = []
+    for i, (pos, nrm, uv, tri) in enumerate(meshes):
+        mat = S.Material((0.1,) * 3, (0.7,) * 3, (0.2,) * 3, 1.0, i % 2, (i + 1) % 2)
+        objs.append(S.ObjectDesc(pos, nrm, uv, [S.MeshDesc(S._tris9(tri), 0)], [mat]))
+    rng = np.random.Generator(np.random.PCG64(42))
+    reqs = []
+    for k in range(24):
+        oi = int(rng.integers(0, 3))
+        w, h = [(64, 64), (160, 90), (256, 256), (333, 200), (512, 300)][int(rng.integers(0, 5))]
+        az, el, dist = rng.uniform(0, 2 * math.pi), rng.uniform(0.1, 1.0), rng.uniform(2.5, 4.0)
+        cam = (dist * math.cos(el) * math.sin(az), dist * math.sin(el), dist * math.cos(el) * math.cos(az))
+        light = [(3.0 * math.sin(az + 1), 4.0, 3.0 * math.cos(az + 1))]
+        reqs.append((oi, w, h, cam, light, [2, 5, 32][k % 3], [float("inf"), 100000.0][k % 2]))
+    return objs, texs, reqs
+
+
+def _alone(objs, texs, reqs):
+    """Reference frames: each request rendered alone through Scene/Canvas on its own context."""
+    from draw_gb300 import renderer as R
+
+    ctx = R.Context(0)
+    tm = [R.TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in texs]
+    obs = [R.upload_object(o, tm, ctx) for o in objs]
+    out = []
+    for oi, w, h, cam, light, e, clear in reqs:
+        sc = R.Scene(w, h, ctx)
+        sc.camera.reset(cam, tuple(-c for c in cam), float(np.float32(w) / np.float32(h)), -0.5, -100.0, 60.0)
+        sc.set_lights(light)
+        sc.set_exponent(e)
+        sc.add_obj(obs[oi])
+        cv = R.Canvas(w, h, ctx)
+        cv.init_depth(clear)
+        sc.render(cv)
+        out.append(cv.read())
+    ctx.close()
+    return out
+
+
+def test_server_mix_equals_alone(gpu_ctx):
+    from draw_gb300 import renderer as R
+
+    objs, texs, reqs = _pool()
+    ref = _alone(objs, texs, reqs)
+    ctx = R.Context(0)
+    tm = [R.TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in texs]
+    obs = [R.upload_object(o, tm, ctx) for o in objs]
+    srv = R.Server(ctx, budget_bytes=1 << 30, max_batch=8, streams=3)
+    tickets = [None] * len(reqs)
+
+    def submit(part):
+        for k in part:
+            oi, w, h, cam, light, e, clear = reqs[k]
+            tickets[k] = srv.submit(R.Server.request(obs[oi], w, h, cam, tuple(-c for c in cam), -0.5, -100.0, 60.0,
+                                                     light, e, clear))
+
+    th = [threading.Thread(target=submit, args=(range(i, len(reqs), 2),)) for i in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for k, (oi, w, h, *_r) in enumerate(reqs):
+        bgra, depth, lat = srv.wait(tickets[k], w, h, read=True)
+        p = compare(ref[k], (bgra, depth), reqs[k][6])
+        assert p.ok and p.colour_max_lsb <= COLOUR_TOL_LSB, f"request {k}: {describe(p)}"
+        assert lat > 0
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["error"] == 0
+    assert st["batches"] < len(reqs)  # requests were batched together
+    srv.close()
+    ctx.close()
+
+
+def test_server_admission_respects_budget(gpu_ctx):
+    from draw_gb300 import renderer as R
+
+    objs, texs, _ = _pool()
+    ctx = R.Context(0)
+    tm = [R.TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in texs]
+    ob = R.upload_object(objs[1], tm, ctx)
+    frame_bytes = 256 * 256 * 16
+    budget = 24 << 20
+    srv = R.Server(ctx, budget_bytes=budget, max_batch=16, streams=2)
+    # a frame that can never fit is refused at submission
+    with pytest.raises(R.DrawError) as e:
+        srv.submit(R.Server.request(ob, 4096, 4096, (0, 1, 3), (0, -1, -3), -0.5, -100.0, 60.0, [(2, 4, 3)]))
+    assert e.value.status == 7
+    ts = [srv.submit(R.Server.request(ob, 256, 256, (0.2 * k, 1, 3), (-0.2 * k, -1, -3), -0.5, -100.0, 60.0,
+                                      [(2, 4, 3)], discard=True)) for k in range(40)]
+    for t in ts:
+        srv.wait(t)
+    st = srv.stats()
+    assert st["completed"] == 40 and st["error"] == 0
+    assert 0 < st["peak_bytes"] <= budget
+    assert frame_bytes * 40 > budget  # the requests did not fit at once
+    srv.close()
+    ctx.close()
