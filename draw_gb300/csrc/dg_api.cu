@@ -550,9 +550,9 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     if (S.timing) DG_CUDA(cudaEventRecord(S.ev[0], S.stream));
     DG_CUDA(dg_launch_vertex(job, S.stream));
     if (S.timing) DG_CUDA(cudaEventRecord(S.ev[1], S.stream));
-    DG_CUDA(dg_launch_setup_raster(job, c->nsm, S.stream));
+    DG_CUDA(dg_launch_setup_raster(job, (unsigned)c->nsm * S.setup_blocks_per_sm, S.stream));
     if (S.timing) DG_CUDA(cudaEventRecord(S.ev[2], S.stream));
-    DG_CUDA(dg_launch_queue_raster(job, c->nsm, S.stream));
+    DG_CUDA(dg_launch_queue_raster(job, (unsigned)c->nsm * S.queue_blocks_per_sm, S.stream));
     if (S.timing) DG_CUDA(cudaEventRecord(S.ev[3], S.stream));
     DG_CUDA(dg_launch_resolve(job, S.stream));
     if (S.timing) {
@@ -683,6 +683,25 @@ dg_status dg_ctx_kernel_times(dg_ctx* c, float* ms, int32_t n) {
     if (!c->main.ev_valid) return DG_E_INVALID;
     DG_CUDA(cudaEventSynchronize(c->main.ev[4]));
     for (int i = 0; i < n && i < 4; i++) DG_CUDA(cudaEventElapsedTime(&ms[i], c->main.ev[i], c->main.ev[i + 1]));
+    return DG_OK;
+}
+
+dg_status dg_ctx_set_tuning(dg_ctx* c, const dg_tuning* t) {
+    if (!c || !t) return DG_E_INVALID;
+    if (t->small_max_px > 4096 || t->setup_blocks_per_sm < 1 || t->setup_blocks_per_sm > 64 ||
+        t->queue_blocks_per_sm < 1 || t->queue_blocks_per_sm > 64)
+        return DG_E_INVALID;
+    c->main.small_max_px = t->small_max_px;
+    c->main.setup_blocks_per_sm = t->setup_blocks_per_sm;
+    c->main.queue_blocks_per_sm = t->queue_blocks_per_sm;
+    return DG_OK;
+}
+
+dg_status dg_ctx_get_tuning(dg_ctx* c, dg_tuning* t) {
+    if (!c || !t) return DG_E_INVALID;
+    t->small_max_px = c->main.small_max_px;
+    t->setup_blocks_per_sm = c->main.setup_blocks_per_sm;
+    t->queue_blocks_per_sm = c->main.queue_blocks_per_sm;
     return DG_OK;
 }
 

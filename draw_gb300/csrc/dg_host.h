@@ -114,7 +114,9 @@ struct JobSlot {
     uint32_t* d_queue_base = nullptr;
     size_t queue_cap = 0;
     size_t queue_base_cap = 0;
-    uint32_t small_max_px = DG_SMALL_MAX_PX;
+    uint32_t small_max_px = DG_SMALL_MAX_PX;  // dg_tuning knobs
+    uint32_t setup_blocks_per_sm = DG_SETUP_BLOCKS_PER_SM;
+    uint32_t queue_blocks_per_sm = DG_QUEUE_BLOCKS_PER_SM;
     unsigned long long* d_counters = nullptr;  // [0] queue counter, [1] covered px, [2] overflow
     uint32_t* d_err = nullptr;
     static const int kStage = 4;  // pinned staging ring for job descriptors

@@ -115,8 +115,11 @@ struct DgJobDev {
 
 // Host-side launchers (dg_kernels.cu).
 cudaError_t dg_launch_vertex(const DgJobDev& job, cudaStream_t s);
-cudaError_t dg_launch_setup_raster(const DgJobDev& job, int nsm, cudaStream_t s);
-cudaError_t dg_launch_queue_raster(const DgJobDev& job, int nsm, cudaStream_t s);
+// max_blocks / blocks: grid size in 256-thread blocks (the setup grid is also capped by the work).
+cudaError_t dg_launch_setup_raster(const DgJobDev& job, unsigned max_blocks, cudaStream_t s);
+cudaError_t dg_launch_queue_raster(const DgJobDev& job, unsigned blocks, cudaStream_t s);
+#define DG_SETUP_BLOCKS_PER_SM 16u
+#define DG_QUEUE_BLOCKS_PER_SM 8u
 cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s);
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,
                            int fill_colour, int fill_depth, cudaStream_t s);

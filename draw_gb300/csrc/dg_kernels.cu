@@ -451,7 +451,13 @@ __device__ __forceinline__ void warp_flat_raster(const DgJobDev& job, const RTri
     }
 }
 
+// Kernels launched with programmatic dependent launch start before the previous
+// kernel of the stream has finished; this waits until it has completed and its
+// memory operations are visible.
+__device__ __forceinline__ void wait_previous_kernel() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
+    wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < job.total_tri; base += stride) {
@@ -467,33 +473,35 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             const DgFrameDev& fr = job.frames[sg.frame];
             t = g - sg.tri_begin;
             tp = __ldg(sg.tri_pos + t);
-            float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-            V3 a = {pa.x, pa.y, pa.z}, b = {pb.x, pb.y, pb.z}, c = {pc.x, pc.y, pc.z};
-            // back-face culling, scene/mod.rs:1016-1027 (Triangle::calc_normal, get_center)
-            V3 n = vcross(vsub(b, a), vsub(c, b));
-            V3 zero = {0.0f, 0.0f, 0.0f};
-            V3 ctr = vdiv(vadd(vadd(vadd(zero, a), b), c), 3.0f);
-            V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
-            if (vdot(vsub(cam, ctr), n) > 0.0f || isnan(vdot(vsub(cam, ctr), n))) {
-                r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
-                r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
-                r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
-                uint32_t m0 = __float_as_uint(r[0].w), m1 = __float_as_uint(r[1].w), m2 = __float_as_uint(r[2].w);
-                uint32_t le = m0 & m1 & m2;
-                uint32_t gt = m0 & m1 & m2;
-                if ((le >> 8) & 0x3Cu) {
-                    nout = 0;  // some lateral plane has all three f <= 0
-                } else if ((gt & 0x3u) == 0x3u) {
-                    nout = 1;  // inside near and far: the triangle passes unchanged
-                } else {
-                    ClipProg P;
-                    build_clip(fr, a, b, c, P);
-                    nout = P.nout;
-                    clipped = true;
-                }
-                if (nout > 0) {  // its vertices need light/halfway vectors for shading
-                    const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
-                    for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+            // The lateral trivial reject (Triangle::clip_against_planes, scene/mod.rs:59-66) and
+            // the back-face test (:1016-1027) are both pure predicates, so testing the cheap one
+            // first gives the same surviving set: the plane-sign masks of the vertex records
+            // reject most off-screen triangles before their positions are gathered.
+            r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
+            r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
+            r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
+            const uint32_t m = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
+            if (((m >> 8) & 0x3Cu) == 0u) {  // no lateral plane has all three f <= 0
+                float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
+                V3 a = {pa.x, pa.y, pa.z}, b = {pb.x, pb.y, pb.z}, c = {pc.x, pc.y, pc.z};
+                // back-face culling: Triangle::calc_normal, get_center; skip when (cam - centre) . n <= 0
+                V3 n = vcross(vsub(b, a), vsub(c, b));
+                V3 zero = {0.0f, 0.0f, 0.0f};
+                V3 ctr = vdiv(vadd(vadd(vadd(zero, a), b), c), 3.0f);
+                V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
+                if (!(vdot(vsub(cam, ctr), n) <= 0.0f)) {
+                    if ((m & 0x3u) == 0x3u) {
+                        nout = 1;  // inside near and far: the triangle passes unchanged
+                    } else {
+                        ClipProg P;
+                        build_clip(fr, a, b, c, P);
+                        nout = P.nout;
+                        clipped = true;
+                    }
+                    if (nout > 0) {  // its vertices need light/halfway vectors for shading
+                        const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
+                        for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+                    }
                 }
             }
         }
@@ -595,6 +603,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
 // row-major in units of DG_UNIT_PX and spread over all warps. A warp keeps its
 // current record (and edge constants) while consecutive units belong to it.
 __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
+    wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -766,7 +775,8 @@ __device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint3
 
 __global__ void __launch_bounds__(256) k_resolve(const DgJobDev job) {
     __shared__ float inv255[256];
-    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
+    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);  // independent of the previous kernel
+    wait_previous_kernel();
     __syncthreads();
     const uint32_t tile = blockIdx.x;
     const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
@@ -828,22 +838,37 @@ cudaError_t dg_launch_vertex(const DgJobDev& job, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t dg_launch_setup_raster(const DgJobDev& job, int nsm, cudaStream_t s) {
-    if (job.total_tri == 0) return cudaSuccess;
-    k_setup_raster<<<grid_for(job.total_tri, (unsigned)nsm * 16u), 256, 0, s>>>(job);
-    return cudaGetLastError();
+// Programmatic dependent launch: the kernel may be scheduled while the previous
+// kernel of the stream drains; it calls wait_previous_kernel() before reading
+// anything that kernel wrote.
+cudaError_t launch_dependent(void (*kern)(DgJobDev), unsigned grid, unsigned block, const DgJobDev& job,
+                             cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, job);
 }
 
-cudaError_t dg_launch_queue_raster(const DgJobDev& job, int nsm, cudaStream_t s) {
+cudaError_t dg_launch_setup_raster(const DgJobDev& job, unsigned max_blocks, cudaStream_t s) {
     if (job.total_tri == 0) return cudaSuccess;
-    k_queue_raster<<<(unsigned)nsm * 8u, 256, 0, s>>>(job);
-    return cudaGetLastError();
+    return launch_dependent(k_setup_raster, grid_for(job.total_tri, max_blocks < 1u ? 1u : max_blocks), 256, job, s);
+}
+
+cudaError_t dg_launch_queue_raster(const DgJobDev& job, unsigned blocks, cudaStream_t s) {
+    if (job.total_tri == 0) return cudaSuccess;
+    return launch_dependent(k_queue_raster, blocks < 1u ? 1u : blocks, 256, job, s);
 }
 
 cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s) {
     if (job.total_tiles == 0) return cudaSuccess;
-    k_resolve<<<job.total_tiles, 256, 0, s>>>(job);
-    return cudaGetLastError();
+    return launch_dependent(k_resolve, job.total_tiles, 256, job, s);
 }
 
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,

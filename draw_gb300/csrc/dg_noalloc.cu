@@ -214,8 +214,8 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     NA_CUDA(dg_launch_vis_reset(reinterpret_cast<uint64_t*>(base + kOffVis), npx, s));
 
     NA_CUDA(dg_launch_vertex(job, s));
-    NA_CUDA(dg_launch_setup_raster(job, nsm, s));
-    NA_CUDA(dg_launch_queue_raster(job, nsm, s));
+    NA_CUDA(dg_launch_setup_raster(job, (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM, s));
+    NA_CUDA(dg_launch_queue_raster(job, (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM, s));
     NA_CUDA(dg_launch_resolve(job, s));
 
     if (status_out) {

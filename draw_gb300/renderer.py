@@ -38,6 +38,8 @@ SIGNATURES = {
     "dg_ctx_set_timing": (_i32, [_P, _i32]),
     "dg_ctx_kernel_times": (_i32, [_P, _P, _i32]),
     "dg_ctx_last_stats": (_i32, [_P, _P, _i32]),
+    "dg_ctx_set_tuning": (_i32, [_P, _P]),
+    "dg_ctx_get_tuning": (_i32, [_P, _P]),
     "dg_texmap_create": (_i32, [_P, _P, _u64, _u64, _u64, _u64, _P]),
     "dg_object_create": (_i32, [_P, _P, _u64, _P, _u64, _P, _u64, _P, _u64, _P, _u64, _P]),
     "dg_object_destroy": (_i32, [_P, _i32]),
@@ -183,6 +185,22 @@ class Context:
         ms = (ctypes.c_float * 4)()
         _chk(self.lib.dg_ctx_kernel_times(self.h, ms, 4), "kernel_times")
         return dict(zip(["vertex", "setup_raster", "queue_raster", "resolve"], list(ms)))
+
+    def set_tuning(self, small_max_px: int = None, setup_blocks_per_sm: int = None, queue_blocks_per_sm: int = None):
+        """Raster knobs: in-warp raster threshold (bounding-box pixels) and grid sizes per SM.
+        None keeps the current value. Results do not depend on them; only speed does."""
+        t = self.get_tuning()
+        for k, v in (("small_max_px", small_max_px), ("setup_blocks_per_sm", setup_blocks_per_sm),
+                     ("queue_blocks_per_sm", queue_blocks_per_sm)):
+            if v is not None:
+                t[k] = int(v)
+        raw = (ctypes.c_uint32 * 3)(t["small_max_px"], t["setup_blocks_per_sm"], t["queue_blocks_per_sm"])
+        _chk(self.lib.dg_ctx_set_tuning(self.h, raw), "set_tuning")
+
+    def get_tuning(self) -> dict:
+        raw = (ctypes.c_uint32 * 3)()
+        _chk(self.lib.dg_ctx_get_tuning(self.h, raw), "get_tuning")
+        return dict(zip(["small_max_px", "setup_blocks_per_sm", "queue_blocks_per_sm"], list(raw)))
 
     def last_stats(self) -> dict:
         v = (ctypes.c_uint64 * 8)()

@@ -79,6 +79,20 @@ void* dg_ctx_stream(dg_ctx* ctx);
  * "queue_raster", "resolve". Enabled with dg_ctx_set_timing(ctx, 1). */
 dg_status dg_ctx_set_timing(dg_ctx* ctx, int32_t enable);
 dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
+/* Launch-shape knobs of the raster passes (chosen by draw_gb300.autotune):
+ * small_max_px: triangles whose clipped bounding box has at most this many
+ * pixels are rasterized by the warp that sets them up, the others go to the
+ * load-balanced queue pass (0 = all queued, max 4096); setup_blocks_per_sm and
+ * queue_blocks_per_sm: grid sizes of those two passes in 256-thread blocks per
+ * SM (1..64). Results do not depend on them. */
+typedef struct {
+    uint32_t small_max_px;
+    uint32_t setup_blocks_per_sm;
+    uint32_t queue_blocks_per_sm;
+} dg_tuning;
+dg_status dg_ctx_set_tuning(dg_ctx* ctx, const dg_tuning* t);
+dg_status dg_ctx_get_tuning(dg_ctx* ctx, dg_tuning* t);
+
 /* Counters of the last render: [0] vertices, [1] input triangles, [2] triangles queued
  * for the load-balanced raster pass, [3] their 32-pixel work units, [4] covered pixels
  * (written by resolve), [5] queued triangles rasterized in place because the queue was

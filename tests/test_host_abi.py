@@ -139,3 +139,17 @@ def test_host_only_context_refuses_device_work(lib):
     assert lib.dg_scene_set_lights(h, 0, None, 0) == 1
     assert lib.dg_status_string(3) == b"texel offset outside the texture map"
     lib.dg_ctx_destroy(h)
+
+
+def test_tuning_round_trip_and_validation(lib):
+    h = host_ctx(lib)
+    t = (ctypes.c_uint32 * 3)()
+    assert lib.dg_ctx_get_tuning(h, t) == 0
+    assert list(t) == [32, 16, 8]
+    assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 3)(0, 1, 64)) == 0
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64]
+    for bad in ((4097, 16, 8), (32, 0, 8), (32, 16, 65)):
+        assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 3)(*bad)) == 1
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64]
+    assert lib.dg_ctx_set_tuning(h, None) == 1
+    lib.dg_ctx_destroy(h)
