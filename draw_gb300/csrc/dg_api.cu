@@ -313,8 +313,8 @@ dg_status slot_init(dg_ctx* c, JobSlot& s, cudaStream_t stream) {
     (void)c;
     s.stream = stream;
     for (int i = 0; i < JobSlot::kStage; i++) DG_CUDA(cudaEventCreateWithFlags(&s.stage_ev[i], cudaEventDisableTiming));
-    for (int i = 0; i < 5; i++) DG_CUDA(cudaEventCreate(&s.ev[i]));
-    dg_status e = dalloc(&s.d_counters, 4);
+    for (int i = 0; i <= DG_NKERNELS; i++) DG_CUDA(cudaEventCreate(&s.ev[i]));
+    dg_status e = dalloc(&s.d_counters, DG_NCOUNTERS);
     if (e) return e;
     e = dalloc(&s.d_err, 1);
     if (e) return e;
@@ -328,7 +328,11 @@ void slot_free(JobSlot& s) {
     dfree(s.d_vshade);
     dfree(s.d_vmark);
     dfree(s.d_queue);
-    dfree(s.d_queue_base);
+    dfree(s.d_items);
+    dfree(s.d_surv);
+    dfree(s.d_rec_of);
+    dfree(s.d_trec);
+    dfree(s.d_shade);
     dfree(s.d_counters);
     dfree(s.d_err);
     for (int i = 0; i < JobSlot::kStage; i++) {
@@ -338,7 +342,7 @@ void slot_free(JobSlot& s) {
         if (s.stage_ev[i]) cudaEventDestroy(s.stage_ev[i]);
         s.stage_ev[i] = nullptr;
     }
-    for (int i = 0; i < 5; i++) {
+    for (int i = 0; i <= DG_NKERNELS; i++) {
         if (s.ev[i]) cudaEventDestroy(s.ev[i]);
         s.ev[i] = nullptr;
     }
@@ -367,6 +371,8 @@ dg_status sync_tex_table(dg_ctx* c, cudaStream_t stream) {
         t[i].comps = c->tex[i].comps;
         t[i].fw = (float)c->tex[i].w;
         t[i].fh = (float)c->tex[i].h;
+        t[i].small = dg_tex_small(c->tex[i].len, c->tex[i].w, c->tex[i].h);
+        t[i].pad[0] = t[i].pad[1] = 0;
     }
     DG_CUDA(cudaStreamSynchronize(stream));
     if (c->d_tex_cap < t.size()) {
@@ -388,19 +394,26 @@ size_t queue_records(uint64_t total_tri) {
     return std::min<size_t>(std::max<size_t>(1u << 16, (size_t)total_tri), (1u << 24) - 1);
 }
 
-uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L) {
+// Triangle records: one per cull survivor plus room for clip outputs (the
+// resolve pass shades the pixels of triangles without a record the long way).
+size_t trec_records(uint64_t total_tri) { return (size_t)std::min<uint64_t>(dg_trec_cap(total_tri), 0xFFFFFFF0ull); }
+
+uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L, uint64_t P) {
     auto cap_after = [](size_t cap, const void* p, size_t need) -> size_t {
         return (cap >= need && p) ? cap : std::max(need, cap * 3 / 2);
     };
     if (L == 0) L = 1;
     const size_t vrec = cap_after(s.vrec_cap, s.d_vrec, std::max<uint64_t>(V, 1));
-    const size_t vshade = cap_after(s.vshade_cap, s.d_vshade, std::max<uint64_t>(V * L * 2, 1));
+    const size_t vshade = cap_after(s.vshade_cap, s.d_vshade, (V + dg_vrow_extra(T)) * L * 2);
     const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>((V + 31) / 32, 1));
     const size_t q = cap_after(s.queue_cap, s.d_queue, queue_records(T));
-    const size_t qb = (s.queue_cap >= queue_records(T) && s.d_queue) ? s.queue_base_cap
-                                                                     : cap_after(s.queue_base_cap, s.d_queue_base, q);
+    const size_t qb = cap_after(s.items_cap, s.d_items, dg_items_cap(q));
+    const size_t sv = cap_after(s.surv_cap, s.d_surv, std::max<uint64_t>(T, 1));
+    const size_t ro = cap_after(s.rec_of_cap, s.d_rec_of, std::max<uint64_t>(T, 1));
+    const size_t tr = cap_after(s.trec_cap, s.d_trec, trec_records(T));
+    const size_t sh = cap_after(s.shade_cap, s.d_shade, std::max<uint64_t>(P, 1));
     return vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + q * sizeof(DgQueueRec) +
-           qb * sizeof(uint32_t);
+           qb * sizeof(uint2) + (sv + ro) * sizeof(uint32_t) + tr * sizeof(DgTriRec) + sh * sizeof(uint2);
 }
 
 dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n) {
@@ -409,7 +422,7 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     if (e) return e;
     std::vector<DgFrameDev> frames(n);
     std::vector<DgSegDev> segs;
-    uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0;
+    uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0, total_px = 0;
     uint32_t stride = 1;
     for (uint32_t i = 0; i < n; i++) {
         Scene& s = *scenes[i];  // frame_setup updates the camera basis, as Scene::render does
@@ -445,6 +458,9 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
         f.tile_begin = (uint32_t)total_tiles;
         f.tiles_x = (uint32_t)((tg.w + DG_TILE_W - 1) / DG_TILE_W);
         total_tiles += (uint64_t)f.tiles_x * ((tg.h + DG_TILE_H - 1) / DG_TILE_H);
+        f.pix_begin = (uint32_t)total_px;
+        total_px += tg.w * tg.h;
+        if (total_px >= 0x80000000ull) return DG_E_LIMIT;  // job-wide pixel indices use 31 bits
         uint64_t seq = 0;
         for (int32_t oid : s.objects) {
             Object& o = c->objects[oid];
@@ -482,7 +498,16 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     if (e) return e;
     e = grow(S, &S.d_vrec, &S.vrec_cap, std::max<uint64_t>(total_vtx, 1));
     if (e) return e;
-    e = grow(S, &S.d_vshade, &S.vshade_cap, std::max<uint64_t>(total_vtx * stride * 2, 1));
+    const uint64_t vrow_extra = dg_vrow_extra(total_tri);
+    e = grow(S, &S.d_vshade, &S.vshade_cap, (total_vtx + vrow_extra) * stride * 2);
+    if (e) return e;
+    e = grow(S, &S.d_surv, &S.surv_cap, std::max<uint64_t>(total_tri, 1));
+    if (e) return e;
+    e = grow(S, &S.d_rec_of, &S.rec_of_cap, std::max<uint64_t>(total_tri, 1));
+    if (e) return e;
+    e = grow(S, &S.d_trec, &S.trec_cap, trec_records(total_tri));
+    if (e) return e;
+    e = grow(S, &S.d_shade, &S.shade_cap, std::max<uint64_t>(total_px, 1));
     if (e) return e;
     const size_t want_mark = std::max<uint64_t>((total_vtx + 31) / 32, 1);
     if (S.vmark_cap < want_mark) {
@@ -494,7 +519,7 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     if (S.queue_cap < want_queue) {
         e = grow(S, &S.d_queue, &S.queue_cap, want_queue);
         if (e) return e;
-        e = grow(S, &S.d_queue_base, &S.queue_base_cap, S.queue_cap);
+        e = grow(S, &S.d_items, &S.items_cap, dg_items_cap(S.queue_cap));
         if (e) return e;
     }
 
@@ -532,33 +557,37 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     job.shade_stride = stride;
     job.vrec = S.d_vrec;
     job.vshade = S.d_vshade;
+    job.vrow_extra = (uint32_t)std::min<uint64_t>(S.vshade_cap / (2ull * stride) - total_vtx, 0xFFFFFFF0ull);
     job.vmark = S.d_vmark;
+    job.surv = S.d_surv;
+    job.rec_of = S.d_rec_of;
+    job.trec = S.d_trec;
+    job.trec_cap = (uint32_t)std::min<size_t>(S.trec_cap, 0xFFFFFFF0ull);
+    if (S.record_limit) job.trec_cap = std::min(job.trec_cap, S.record_limit);
     job.queue = S.d_queue;
-    job.queue_base = S.d_queue_base;
+    job.items = S.d_items;
+    job.items_cap = (uint32_t)std::min<size_t>(S.items_cap, 0xFFFFFFF0ull);
     job.queue_cap = (uint32_t)std::min<size_t>(S.queue_cap, (1u << 24) - 1);
     job.small_max_px = S.small_max_px;
-    job.queue_counter = S.d_counters;
-    job.stats = S.d_counters + 1;
+    job.cnt = S.d_counters;
+    job.total_px = (uint32_t)total_px;
+    job.shade_list = S.d_shade;
     job.tex = c->d_tex;
+    job.ntex = (uint32_t)c->tex.size();
     job.err = S.d_err;
     S.last_vtx = total_vtx;
     S.last_tri = total_tri;
     S.last_h2d = need;
-    S.last_launches = (total_vtx ? 1 : 0) + (total_tri ? 2 : 0) + (total_tiles ? 1 : 0);
+    S.last_launches = (total_vtx ? 1 : 0) + (total_tri ? 3 : 0) + (total_tiles ? 1 : 0) + (total_px ? 1 : 0);
 
-    DG_CUDA(cudaMemsetAsync(S.d_counters, 0, 3 * sizeof(unsigned long long), S.stream));
-    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[0], S.stream));
-    DG_CUDA(dg_launch_vertex(job, S.stream));
-    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[1], S.stream));
-    DG_CUDA(dg_launch_setup_raster(job, (unsigned)c->nsm * S.setup_blocks_per_sm, S.stream));
-    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[2], S.stream));
-    DG_CUDA(dg_launch_queue_raster(job, (unsigned)c->nsm * S.queue_blocks_per_sm, S.stream));
-    if (S.timing) DG_CUDA(cudaEventRecord(S.ev[3], S.stream));
-    DG_CUDA(dg_launch_resolve(job, S.stream));
-    if (S.timing) {
-        DG_CUDA(cudaEventRecord(S.ev[4], S.stream));
-        S.ev_valid = true;
-    }
+    DG_CUDA(cudaMemsetAsync(S.d_counters, 0, DG_NCOUNTERS * sizeof(unsigned long long), S.stream));
+    DgLaunchCfg cfg;
+    cfg.cull_blocks = (unsigned)c->nsm * S.cull_blocks_per_sm;
+    cfg.setup_blocks = (unsigned)c->nsm * S.setup_blocks_per_sm;
+    cfg.queue_blocks = (unsigned)c->nsm * S.queue_blocks_per_sm;
+    cfg.shade_blocks = (unsigned)c->nsm * DG_SHADE_BLOCKS_PER_SM;
+    DG_CUDA(dg_launch_job(job, cfg, S.stream, S.timing ? S.ev : nullptr));
+    if (S.timing) S.ev_valid = true;
     return DG_OK;
 }
 
@@ -681,19 +710,23 @@ dg_status dg_ctx_kernel_times(dg_ctx* c, float* ms, int32_t n) {
     if (!c || !ms || n < 0) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;
     if (!c->main.ev_valid) return DG_E_INVALID;
-    DG_CUDA(cudaEventSynchronize(c->main.ev[4]));
-    for (int i = 0; i < n && i < 4; i++) DG_CUDA(cudaEventElapsedTime(&ms[i], c->main.ev[i], c->main.ev[i + 1]));
+    DG_CUDA(cudaEventSynchronize(c->main.ev[DG_NKERNELS]));
+    for (int i = 0; i < n && i < DG_NKERNELS; i++)
+        DG_CUDA(cudaEventElapsedTime(&ms[i], c->main.ev[i], c->main.ev[i + 1]));
     return DG_OK;
 }
 
 dg_status dg_ctx_set_tuning(dg_ctx* c, const dg_tuning* t) {
     if (!c || !t) return DG_E_INVALID;
-    if (t->small_max_px > 4096 || t->setup_blocks_per_sm < 1 || t->setup_blocks_per_sm > 64 ||
-        t->queue_blocks_per_sm < 1 || t->queue_blocks_per_sm > 64)
+    auto bad = [](uint32_t b) { return b < 1 || b > 64; };
+    if (t->small_max_px > 4096 || bad(t->setup_blocks_per_sm) || bad(t->queue_blocks_per_sm) ||
+        bad(t->cull_blocks_per_sm))
         return DG_E_INVALID;
     c->main.small_max_px = t->small_max_px;
     c->main.setup_blocks_per_sm = t->setup_blocks_per_sm;
     c->main.queue_blocks_per_sm = t->queue_blocks_per_sm;
+    c->main.cull_blocks_per_sm = t->cull_blocks_per_sm;
+    c->main.record_limit = t->record_limit;
     return DG_OK;
 }
 
@@ -702,6 +735,8 @@ dg_status dg_ctx_get_tuning(dg_ctx* c, dg_tuning* t) {
     t->small_max_px = c->main.small_max_px;
     t->setup_blocks_per_sm = c->main.setup_blocks_per_sm;
     t->queue_blocks_per_sm = c->main.queue_blocks_per_sm;
+    t->cull_blocks_per_sm = c->main.cull_blocks_per_sm;
+    t->record_limit = c->main.record_limit;
     return DG_OK;
 }
 
@@ -710,11 +745,20 @@ dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
     if (c->device < 0) return DG_E_CUDA;
     JobSlot& S = c->main;
     DG_CUDA(cudaStreamSynchronize(S.stream));
-    unsigned long long h[3];
+    unsigned long long h[DG_NCOUNTERS];
     DG_CUDA(cudaMemcpy(h, S.d_counters, sizeof(h), cudaMemcpyDeviceToHost));
-    uint64_t v[8] = {S.last_vtx, S.last_tri, h[0] >> DG_PACK_SHIFT, h[0] & ((1ull << DG_PACK_SHIFT) - 1ull),
-                     h[1], h[2], S.last_h2d, S.last_launches};
-    for (int i = 0; i < n && i < 8; i++) out[i] = v[i];
+    const uint64_t v[11] = {S.last_vtx,
+                            S.last_tri,
+                            h[DG_CNT_QUEUE] >> DG_PACK_SHIFT,
+                            h[DG_CNT_UNITS],
+                            h[DG_CNT_COVERED],
+                            h[DG_CNT_INPLACE],
+                            S.last_h2d,
+                            S.last_launches,
+                            h[DG_CNT_SURV],
+                            h[DG_CNT_TREC],
+                            h[DG_CNT_VROW]};
+    for (int i = 0; i < n && i < 11; i++) out[i] = v[i];
     return DG_OK;
 }
 

@@ -111,13 +111,23 @@ struct JobSlot {
     uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
     size_t vmark_cap = 0;
     DgQueueRec* d_queue = nullptr;
-    uint32_t* d_queue_base = nullptr;
+    uint2* d_items = nullptr;  // raster work items
     size_t queue_cap = 0;
-    size_t queue_base_cap = 0;
+    size_t items_cap = 0;
+    uint32_t* d_surv = nullptr;  // cull survivors
+    size_t surv_cap = 0;
+    uint32_t* d_rec_of = nullptr;  // first triangle record of each survivor
+    size_t rec_of_cap = 0;
+    DgTriRec* d_trec = nullptr;
+    size_t trec_cap = 0;
+    uint2* d_shade = nullptr;  // shade list (one entry per pixel of the job)
+    size_t shade_cap = 0;
     uint32_t small_max_px = DG_SMALL_MAX_PX;  // dg_tuning knobs
     uint32_t setup_blocks_per_sm = DG_SETUP_BLOCKS_PER_SM;
     uint32_t queue_blocks_per_sm = DG_QUEUE_BLOCKS_PER_SM;
-    unsigned long long* d_counters = nullptr;  // [0] queue counter, [1] covered px, [2] overflow
+    uint32_t cull_blocks_per_sm = DG_CULL_BLOCKS_PER_SM;
+    uint32_t record_limit = 0;
+    unsigned long long* d_counters = nullptr;  // DG_NCOUNTERS job counters (DG_CNT_*)
     uint32_t* d_err = nullptr;
     static const int kStage = 4;  // pinned staging ring for job descriptors
     void* h_stage[kStage] = {};
@@ -126,7 +136,7 @@ struct JobSlot {
     cudaEvent_t stage_ev[kStage] = {};
     int stage = 0;
     bool timing = false;
-    cudaEvent_t ev[5] = {};
+    cudaEvent_t ev[DG_NKERNELS + 1] = {};
     bool ev_valid = false;
     uint64_t last_vtx = 0, last_tri = 0, last_h2d = 0, last_launches = 0;
     uint64_t scratch_bytes = 0;  // device bytes held by the scratch buffers
@@ -158,8 +168,8 @@ dg_status slot_take_errors(JobSlot& s);
 // Uploads the texture table if textures were added.
 dg_status sync_tex_table(dg_ctx* c, cudaStream_t s);
 // Device bytes slot s's scratch will hold after launching a job of V vertices,
-// T triangles and L lights per vertex (same sizing rules as launch_frames).
-uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L);
+// T triangles, L lights per vertex and P pixels (same sizing rules as launch_frames).
+uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L, uint64_t P);
 // Builds and launches one render job over n frames on slot s (asynchronous).
 dg_status launch_frames(dg_ctx* c, JobSlot& s, Scene* const* scenes, const FrameTarget* targets, uint32_t n);
 

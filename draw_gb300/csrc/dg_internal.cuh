@@ -14,6 +14,7 @@
 //                   raster-queue records + their work-unit bases, counters
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -24,30 +25,36 @@
 
 // Triangles whose clipped bounding box has at most this many pixels are
 // rasterized by the warp that set them up (default of DgJobDev.small_max_px);
-// larger ones go to the raster queue, whose pixels are spread over all warps
-// in units of DG_UNIT_PX row-major bounding-box pixels.
+// larger ones go to the raster queue: their row-major bounding-box pixels are
+// cut into units of DG_UNIT_PX (one per lane of a warp) and the units into work
+// items of at most DG_ITEM_UNITS, which the queue pass spreads over all warps.
 #define DG_SMALL_MAX_PX 32u
 #define DG_UNIT_PX 32u
-// Resolve tile: 32 x 8 pixels, one CTA of 256 threads.
+#define DG_ITEM_UNITS 8u
+// Resolve tile: 32 x 32 pixels, one CTA of 256 threads (four rows each).
 #define DG_TILE_W 32u
-#define DG_TILE_H 8u
+#define DG_TILE_H 32u
 #define DG_PACK_SHIFT 40
 
-struct DgTexDev {
+// Device descriptors are 16-byte aligned with sizes that are multiples of 16,
+// so kernels read them with 16-byte loads.
+struct alignas(16) DgTexDev {
     const uint32_t* words;  // image bytes, little-endian in u32 words, one pad word at the end
     uint64_t len;           // image length in bytes
     uint32_t width, height, comps;
     float fw, fh;           // width as f32, height as f32
+    uint32_t small;         // 1 if len < 2^32 and width, height < 2^24 (32-bit texel offsets suffice)
+    uint32_t pad[2];
 };
 
-struct DgMatDev {
+struct alignas(16) DgMatDev {
     float ka[3], kd[3], ks[3];
     float alpha;
     uint32_t map_ka, map_kd;  // indices into the context's texture table
 };
 
 // One frame of a render job (a (scene, canvas) pair).
-struct DgFrameDev {
+struct alignas(16) DgFrameDev {
     float M[4][4];       // viewport * orth * persp * view
     float plane[6][4];   // near, far, right, left, top, bottom: (n.x, n.y, n.z, k)
     float cam[3];
@@ -62,8 +69,19 @@ struct DgFrameDev {
     float* depth;
     uint32_t seg_begin, seg_count;  // this frame's segments (ascending seq_base)
     uint32_t tile_begin, tiles_x;   // this frame's resolve tiles
-    uint32_t pad[2];
+    uint32_t pix_begin;             // job-wide index of this frame's first pixel
+    uint32_t pad[3];
 };
+static_assert(sizeof(DgTexDev) == 48 && sizeof(DgMatDev) == 48, "descriptor sizes");
+inline uint32_t dg_tex_small(uint64_t len, uint64_t w, uint64_t h) {
+    return (len < (1ull << 32) && w < (1ull << 24) && h < (1ull << 24)) ? 1u : 0u;
+}
+static_assert(sizeof(DgFrameDev) % 16 == 0, "frame descriptor size");
+// 16-byte words of DgFrameDev read with vector loads by the kernels.
+static_assert(offsetof(DgFrameDev, plane) == 64 && offsetof(DgFrameDev, cam) == 160 &&
+                  offsetof(DgFrameDev, clear_depth) == 172 && offsetof(DgFrameDev, nlights) == 272 &&
+                  offsetof(DgFrameDev, off_x) == 280 && offsetof(DgFrameDev, off_y) == 284,
+              "frame descriptor layout");
 
 // The opaque triangles and the vertices of one object within one frame.
 struct DgSegDev {
@@ -82,45 +100,103 @@ struct DgSegDev {
     const DgMatDev* mats;
 };
 
-// A triangle queued for the load-balanced raster pass (64 bytes).
-struct DgQueueRec {
-    float ax, ay, bx, by, cx, cy;  // snapped centres
-    float da, db, dc;              // vertex depths
-    uint32_t seq;                  // frame-local key low word
-    uint32_t frame;
-    uint32_t xlo, ylo;             // clipped bounding box origin
-    uint32_t w;                    // bounding box width in pixels
-    uint32_t npx;                  // bounding box pixels
-    uint32_t nunits;               // ceil(npx / DG_UNIT_PX), 0 if the record is rasterized elsewhere
+// Edge constants of one triangle: f_k(x, y) = ((A[k]*x + B[k]*y) + C[k]) - D[k]
+// (canvas.rs:597-616 with the products of the vertex coordinates precomputed;
+// the per-pixel value is the same IEEE result), k = 0: f_bc (alpha), 1: f_ca
+// (beta), 2: f_ab (gama).
+struct DgEdges {
+    float A[3], B[3], C[3], D[3];
+    float den[3];  // f_alpha = f_bc(a), f_beta = f_ca(b), f_gama = f_ab(c)
+    uint32_t tie;  // bit k: den[k] * f_k(-1, -1) > 0 (the reference's tie rule)
 };
+
+// One triangle (or one clip output of it) as the raster and shade passes read
+// it: twelve 16-byte words. Attribute fields hold the three vertices' values
+// in x, y, z (clip outputs: the values VertexAttributes arithmetic gives the
+// new vertices, canvas.rs:242-291); the w slots carry the triangle's material.
+struct alignas(16) DgTriRec {
+    DgEdges e;                    // words 0-3
+    float da, db, dc, ka_x;       // word 4: vertex depths (eye distances)
+    float u[3], ka_y;             // word 5: texture coordinates
+    float v[3], ka_z;             // word 6
+    float nx[3], kd_x;            // words 7-9: normals
+    float ny[3], kd_y;
+    float nz[3], kd_z;
+    uint32_t vrow[3];             // word 10: rows of the light/halfway table of the three vertices
+    float ks_x;
+    float ks_y, ks_z;             // word 11
+    uint32_t map_ka, map_kd;      // texture table indices
+};
+static_assert(sizeof(DgTriRec) == 192, "triangle record size");
+
+// A triangle queued for the load-balanced raster pass (32 bytes).
+struct alignas(16) DgQueueRec {
+    uint32_t rec;     // its DgTriRec
+    uint32_t seq;     // frame-local key low word
+    uint32_t frame;
+    uint32_t xlo, ylo;  // clipped bounding box origin
+    uint32_t w;         // bounding box width in pixels
+    uint32_t npx;       // bounding box pixels
+    uint32_t nunits;    // ceil(npx / DG_UNIT_PX)
+};
+
+#define DG_NONE 0xFFFFFFFFu
+// Job counters (unsigned long long each).
+#define DG_CNT_QUEUE 0    // (queued records << DG_PACK_SHIFT) | work items
+#define DG_CNT_COVERED 1  // covered pixels (entries of the shade list)
+#define DG_CNT_INPLACE 2  // large triangles rasterized by their own lane (queue or record overflow)
+#define DG_CNT_SURV 3     // triangles that passed the cull pass
+#define DG_CNT_TREC 4     // triangle records handed out
+#define DG_CNT_VROW 5     // light/halfway rows handed out to clip vertices
+#define DG_CNT_UNITS 6    // work units of the queued triangles
+#define DG_NCOUNTERS 8
 
 struct DgJobDev {
     const DgFrameDev* frames;
     const DgSegDev* segs;
     uint32_t nframes, nsegs;
     uint32_t total_vtx, total_tri, total_tiles;
-    uint32_t shade_stride;  // lights per vertex row of vshade (max over frames)
+    uint32_t shade_stride;  // lights per row of vshade (max over frames)
     float4* vrec;
-    float4* vshade;
+    float4* vshade;         // rows [0, total_vtx): job vertices; then rows for clip vertices
+    uint32_t vrow_extra;    // rows after total_vtx available to clip vertices
     uint32_t* vmark;        // one bit per job vertex: needs light/halfway vectors (kept zero between jobs)
-    DgQueueRec* queue;
-    uint32_t* queue_base;   // first work unit of each record (ascending)
+    uint32_t* surv;         // [total_tri] job-wide indices of the triangles that passed the cull pass
+    uint32_t* rec_of;       // [total_tri] first DgTriRec of each surviving triangle, or DG_NONE
+    DgTriRec* trec;
+    uint32_t trec_cap;
     uint32_t queue_cap;
+    DgQueueRec* queue;
+    uint2* items;           // work items: (queue record, first unit)
+    uint32_t items_cap;
     uint32_t small_max_px;  // in-warp raster threshold (bounding-box pixels)
-    unsigned long long* queue_counter;  // (records << 40) | work units
-    unsigned long long* stats;          // [0] covered pixels, [1] queued triangles rasterized in place
+    uint32_t total_px;      // pixels of all frames
+    uint2* shade_list;      // [total_px] (job-wide pixel index, key low word) of the covered pixels
+    unsigned long long* cnt;  // DG_NCOUNTERS job counters, zero at the start of the job
     const DgTexDev* tex;
+    uint32_t ntex;          // entries of tex
     uint32_t* err;
 };
 
 // Host-side launchers (dg_kernels.cu).
-cudaError_t dg_launch_vertex(const DgJobDev& job, cudaStream_t s);
-// max_blocks / blocks: grid size in 256-thread blocks (the setup grid is also capped by the work).
-cudaError_t dg_launch_setup_raster(const DgJobDev& job, unsigned max_blocks, cudaStream_t s);
-cudaError_t dg_launch_queue_raster(const DgJobDev& job, unsigned blocks, cudaStream_t s);
-#define DG_SETUP_BLOCKS_PER_SM 16u
+struct DgLaunchCfg {
+    unsigned cull_blocks;   // grid caps / sizes in 256-thread blocks
+    unsigned setup_blocks;
+    unsigned queue_blocks;
+    unsigned shade_blocks;
+};
+#define DG_SETUP_BLOCKS_PER_SM 4u
 #define DG_QUEUE_BLOCKS_PER_SM 8u
-cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s);
+#define DG_CULL_BLOCKS_PER_SM 32u
+#define DG_SHADE_BLOCKS_PER_SM 8u
+#define DG_NKERNELS 6  // vertex, cull, setup_raster, queue_raster, resolve, shade
+// Launches the whole pipeline of one job on stream s. ev, if not null, holds
+// DG_NKERNELS + 1 events recorded around the kernels (per-kernel timing).
+cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev);
+// Scratch rows and records sized for a job of T triangles (shared sizing rule).
+constexpr uint64_t dg_trec_cap(uint64_t T) { return T + 4096u; }
+constexpr uint64_t dg_items_cap(uint64_t queue_cap) { return 2u * queue_cap + 65536u; }
+constexpr uint64_t dg_vrow_extra(uint64_t T) { uint64_t x = 65536u + T / 8u; return x < 6u * T + 6u ? x : 6u * T + 6u; }
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,
                            int fill_colour, int fill_depth, cudaStream_t s);
 cudaError_t dg_launch_vis_reset(uint64_t* vis, uint64_t n, cudaStream_t s);

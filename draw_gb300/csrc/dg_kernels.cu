@@ -1,17 +1,22 @@
 // dg_kernels.cu -- sm_103a kernels of the GB300 rasterizer.
 //
 // Pipeline of one render job (one or many frames), all on one stream:
-//   k_vertex        per position vertex: eye distance, light/halfway vectors,
-//                   projected and snapped screen centre, plane-sign masks
-//                   (scene/mod.rs:917-926, :1047-1058, canvas.rs:585-587)
-//   k_setup_raster  per input triangle: back-face cull, lateral reject,
-//                   near/far clipping, bounding box, edge functions; tiny
-//                   triangles are rasterized by their warp (pixels of all 32
-//                   lanes' boxes flattened with a warp prefix scan), the others
-//                   are queued (scene/mod.rs:933-1063, canvas.rs:585-681)
-//   k_queue_raster  the queued triangles' bounding-box pixels in 32-pixel units
+//   k_vertex        per position vertex: eye distance, projected and snapped
+//                   screen centre, plane-sign masks (scene/mod.rs:917-926,
+//                   :1047-1058, canvas.rs:585-587)
+//   k_cull          per input triangle: lateral and near reject from the sign
+//                   masks, back-face cull; survivors are compacted
+//   k_setup_raster  per survivor: near/far clipping, triangle records, bounding
+//                   box, edge functions; tiny triangles are rasterized by their
+//                   warp (pixels of all 32 lanes' boxes flattened with a warp
+//                   prefix scan), the others are queued (scene/mod.rs:933-1063,
+//                   canvas.rs:585-681)
+//   k_queue_raster  light/halfway vectors of the marked vertices, then the
+//                   queued triangles' bounding-box pixels in 32-pixel units
 //                   spread evenly over all warps
-//   k_resolve       per pixel: the winning fragment is shaded once
+//   k_resolve       per pixel: empty pixels get the clear colour/depth, covered
+//                   ones are compacted into the shade list
+//   k_shade         per covered pixel: the winning fragment is shaded once
 //                   (canvas.rs:682-745, 906-930) and colour/depth are written
 //
 // Exactness. The reference writes a fragment when its depth is strictly below
@@ -122,11 +127,7 @@ __device__ __forceinline__ void project_snap(const DgFrameDev& fr, V3 p, float& 
 // f_xy(x, y) = (((p.y - q.y) * x + (q.x - p.x) * y) + p.x * q.y) - q.x * p.y
 // (canvas.rs:597-616) with the per-edge constants precomputed; the per-pixel
 // result is the same IEEE value.
-struct EdgeSet {
-    float A[3], B[3], C[3], D[3];  // 0: f_bc (alpha), 1: f_ca (beta), 2: f_ab (gama)
-    float den[3];                  // f_alpha, f_beta, f_gama
-    uint32_t tie;                  // bit k: den[k] * f_k(-1,-1) > 0
-};
+using EdgeSet = DgEdges;
 __device__ __forceinline__ float edge_eval(const EdgeSet& e, int k, float x, float y) {
     return fS(fA(fA(fM(e.A[k], x), fM(e.B[k], y)), e.C[k]), e.D[k]);
 }
@@ -351,9 +352,25 @@ __device__ __forceinline__ uint32_t seg_of_tri(const DgJobDev& job, uint32_t g) 
     return last_le(job.nsegs, g, [&](uint32_t i) { return job.segs[i].tri_begin; });
 }
 
-// Light and halfway vectors of job vertex v for every light (scene/mod.rs:920-925).
-// Only vertices of triangles that survive culling and clipping need them, so
-// they are computed after the setup pass for the vertices it marked.
+// Light and halfway vectors of a vertex at world position p for light l
+// (scene/mod.rs:920-925); eye_n = normalize(p - camera).
+__device__ __forceinline__ void light_halfway(const DgFrameDev& fr, V3 p, V3 eye_n, uint32_t l, V3& lt, V3& h) {
+    const V3 L = {fr.light[l][0], fr.light[l][1], fr.light[l][2]};
+    lt = vnormalized(vsub(p, L));
+    h = vnormalized(vadd(lt, eye_n));
+}
+
+// Writes row `row` of the light/halfway table: per light l, float4s 2l and 2l+1
+// hold (lt.x, lt.y, lt.z, h.x) and (h.y, h.z, 0, 0).
+__device__ __forceinline__ void put_shade(const DgJobDev& job, uint32_t row, uint32_t l, V3 lt, V3 h) {
+    float4* dst = job.vshade + ((uint64_t)row * job.shade_stride + l) * 2;
+    dst[0] = make_float4(lt.x, lt.y, lt.z, h.x);
+    dst[1] = make_float4(h.y, h.z, 0.0f, 0.0f);
+}
+
+// Light and halfway vectors of job vertex v for every light. Only vertices of
+// triangles that survive culling and clipping need them, so they are computed
+// after the setup pass for the vertices it marked.
 __device__ __forceinline__ void shade_vertex(const DgJobDev& job, uint32_t v) {
     const uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
     const DgSegDev& sg = job.segs[si];
@@ -363,17 +380,128 @@ __device__ __forceinline__ void shade_vertex(const DgJobDev& job, uint32_t v) {
     const V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
     const V3 eye = vnormalized(vsub(p, cam));
     for (uint32_t l = 0; l < fr.nlights; l++) {
-        V3 L = {fr.light[l][0], fr.light[l][1], fr.light[l][2]};
-        V3 lt = vnormalized(vsub(p, L));
-        V3 h = vnormalized(vadd(lt, eye));
-        float4* dst = job.vshade + ((uint64_t)v * job.shade_stride + l) * 2;
-        dst[0] = make_float4(lt.x, lt.y, lt.z, h.x);
-        dst[1] = make_float4(h.y, h.z, 0.0f, 0.0f);
+        V3 lt, h;
+        light_halfway(fr, p, eye, l, lt, h);
+        put_shade(job, v, l, lt, h);
     }
 }
 
+// Rows of the light/halfway table for the new vertices (ids 3 .. nv-1) of a
+// clipped triangle: the three input vertices' vectors are computed here (the
+// same operations as shade_vertex, so the same values) and carried through the
+// clip program field by field. Row of vertex k: total_vtx + row0 + (k - 3).
+__device__ __noinline__ void clip_shade_rows(const DgJobDev& job, const DgFrameDev& fr, const ClipProg& P,
+                                             uint32_t row0) {
+    const V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
+    V3 eye[3];
+    for (int i = 0; i < 3; i++) eye[i] = vnormalized(vsub(P.pos[i], cam));
+    for (uint32_t l = 0; l < fr.nlights; l++) {
+        float f[6][9];
+        for (int i = 0; i < 3; i++) {
+            V3 lt, h;
+            light_halfway(fr, P.pos[i], eye[i], l, lt, h);
+            f[0][i] = lt.x; f[1][i] = lt.y; f[2][i] = lt.z;
+            f[3][i] = h.x; f[4][i] = h.y; f[5][i] = h.z;
+        }
+        for (int k = 3; k < P.nv; k++)
+            for (int c = 0; c < 6; c++) f[c][k] = fA(f[c][P.p[k]], fM(fS(f[c][P.q[k]], f[c][P.p[k]]), P.t[k]));
+        for (int k = 3; k < P.nv; k++)
+            put_shade(job, job.total_vtx + row0 + (uint32_t)(k - 3), l, V3{f[0][k], f[1][k], f[2][k]},
+                      V3{f[3][k], f[4][k], f[5][k]});
+    }
+}
+
+__device__ __forceinline__ void store_edges(DgTriRec* r, const EdgeSet& e) {
+    float4* d = reinterpret_cast<float4*>(r);
+    d[0] = make_float4(e.A[0], e.A[1], e.A[2], e.B[0]);
+    d[1] = make_float4(e.B[1], e.B[2], e.C[0], e.C[1]);
+    d[2] = make_float4(e.C[2], e.D[0], e.D[1], e.D[2]);
+    d[3] = make_float4(e.den[0], e.den[1], e.den[2], __uint_as_float(e.tie));
+}
+__device__ __forceinline__ void load_edges(const DgTriRec* r, EdgeSet& e) {
+    const float4* s = reinterpret_cast<const float4*>(r);
+    const float4 a = __ldg(s), b = __ldg(s + 1), c = __ldg(s + 2), d = __ldg(s + 3);
+    e.A[0] = a.x; e.A[1] = a.y; e.A[2] = a.z; e.B[0] = a.w;
+    e.B[1] = b.x; e.B[2] = b.y; e.C[0] = b.z; e.C[1] = b.w;
+    e.C[2] = c.x; e.D[0] = c.y; e.D[1] = c.z; e.D[2] = c.w;
+    e.den[0] = d.x; e.den[1] = d.y; e.den[2] = d.z; e.tie = __float_as_uint(d.w);
+}
+
+// Material words of a triangle record: ka, kd, ks and the two texture indices
+// spread over the w slots of words 4-10 and word 11.
+__device__ __forceinline__ void mat_words(const DgSegDev& sg, uint32_t mi, float w[9], uint4& last, const DgJobDev& job) {
+    if (mi >= sg.nmats) {  // never produced by the host API; flagged and shaded as zero material
+        atomicOr(job.err, 1u << DG_E_CUDA);
+        mi = 0;
+    }
+    const float4* mq = reinterpret_cast<const float4*>(sg.mats + mi);
+    const float4 m0 = __ldg(mq), m1 = __ldg(mq + 1), m2 = __ldg(mq + 2);  // ka, kd, ks, alpha, map_ka, map_kd
+    w[0] = m0.x; w[1] = m0.y; w[2] = m0.z;  // ka
+    w[3] = m0.w; w[4] = m1.x; w[5] = m1.y;  // kd
+    w[6] = m1.z;                            // ks.x
+    last = make_uint4(__float_as_uint(m1.w), __float_as_uint(m2.x), __float_as_uint(m2.z), __float_as_uint(m2.w));
+}
+
+// Triangle record of an unclipped triangle (its vertices are the mesh's).
+__device__ __forceinline__ void write_record(const DgJobDev& job, const DgSegDev& sg, uint32_t t, uint4 tp,
+                                             const EdgeSet& e, const float4 r[3], uint32_t rec) {
+    DgTriRec* R = job.trec + rec;
+    store_edges(R, e);
+    const uint4 tuv = __ldg(sg.tri_uv + t), tnr = __ldg(sg.tri_nrm + t);
+    const float2 u0 = __ldg(sg.uv + tuv.x), u1 = __ldg(sg.uv + tuv.y), u2 = __ldg(sg.uv + tuv.z);
+    const float4 n0 = __ldg(sg.nrm + tnr.x), n1 = __ldg(sg.nrm + tnr.y), n2 = __ldg(sg.nrm + tnr.z);
+    float mw[9];
+    uint4 last;
+    mat_words(sg, tp.w, mw, last, job);
+    float4* d = reinterpret_cast<float4*>(R);
+    d[4] = make_float4(r[0].z, r[1].z, r[2].z, mw[0]);
+    d[5] = make_float4(u0.x, u1.x, u2.x, mw[1]);
+    d[6] = make_float4(u0.y, u1.y, u2.y, mw[2]);
+    d[7] = make_float4(n0.x, n1.x, n2.x, mw[3]);
+    d[8] = make_float4(n0.y, n1.y, n2.y, mw[4]);
+    d[9] = make_float4(n0.z, n1.z, n2.z, mw[5]);
+    reinterpret_cast<uint4*>(R)[10] =
+        make_uint4(sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z, __float_as_uint(mw[6]));
+    reinterpret_cast<uint4*>(R)[11] = last;
+}
+
+// Triangle record of clip output o: attribute fields through the clip program.
+__device__ __noinline__ void write_clip_record(const DgJobDev& job, const DgSegDev& sg, uint32_t t, uint4 tp,
+                                               const EdgeSet& e, const RTri& tr, const ClipProg& P, int o,
+                                               uint32_t row0, uint32_t rec) {
+    DgTriRec* R = job.trec + rec;
+    store_edges(R, e);
+    const uint4 tuv = __ldg(sg.tri_uv + t), tnr = __ldg(sg.tri_nrm + t);
+    const float2 u0 = __ldg(sg.uv + tuv.x), u1 = __ldg(sg.uv + tuv.y), u2 = __ldg(sg.uv + tuv.z);
+    const float4 n0 = __ldg(sg.nrm + tnr.x), n1 = __ldg(sg.nrm + tnr.y), n2 = __ldg(sg.nrm + tnr.z);
+    float mw[9];
+    uint4 last;
+    mat_words(sg, tp.w, mw, last, job);
+    float f[3];
+    float4* d = reinterpret_cast<float4*>(R);
+    d[4] = make_float4(tr.da, tr.db, tr.dc, mw[0]);
+    clip_field(P, o, u0.x, u1.x, u2.x, f);
+    d[5] = make_float4(f[0], f[1], f[2], mw[1]);
+    clip_field(P, o, u0.y, u1.y, u2.y, f);
+    d[6] = make_float4(f[0], f[1], f[2], mw[2]);
+    clip_field(P, o, n0.x, n1.x, n2.x, f);
+    d[7] = make_float4(f[0], f[1], f[2], mw[3]);
+    clip_field(P, o, n0.y, n1.y, n2.y, f);
+    d[8] = make_float4(f[0], f[1], f[2], mw[4]);
+    clip_field(P, o, n0.z, n1.z, n2.z, f);
+    d[9] = make_float4(f[0], f[1], f[2], mw[5]);
+    const uint32_t vi[3] = {tp.x, tp.y, tp.z};
+    uint32_t rows[3];
+    for (int i = 0; i < 3; i++) {
+        const int id = P.out[o][i];
+        rows[i] = id < 3 ? sg.vtx_begin + vi[id] : job.total_vtx + row0 + (uint32_t)(id - 3);
+    }
+    reinterpret_cast<uint4*>(R)[10] = make_uint4(rows[0], rows[1], rows[2], __float_as_uint(mw[6]));
+    reinterpret_cast<uint4*>(R)[11] = last;
+}
+
 // ================================================================ kernels
-__global__ void __launch_bounds__(256) k_vertex(const DgJobDev job) {
+__global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < job.total_vtx; v += stride) {
         uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
@@ -393,6 +521,56 @@ __global__ void __launch_bounds__(256) k_vertex(const DgJobDev job) {
             if (f <= 0.0f) mask |= 1u << (8 + pl);
         }
         job.vrec[v] = make_float4(cx, cy, depth, __uint_as_float(mask));
+    }
+}
+
+// Kernels launched with programmatic dependent launch start before the previous
+// kernel of the stream has finished; this waits until it has completed and its
+// memory operations are visible.
+__device__ __forceinline__ void wait_previous_kernel() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Cull pass: one thread per input triangle. A triangle is dropped when one
+// lateral plane has all three vertices at f <= 0 (Triangle::clip_against_planes,
+// scene/mod.rs:59-66), when all three are at f <= 0 for the near plane (the
+// near clip then outputs nothing, :67-87 with ViewPlane::clip :662-690), or when
+// it faces away from the camera (:1016-1027). All three are pure predicates of
+// the triangle, so testing them in this order gives the reference's surviving
+// set; the plane tests read only the vertex records' sign masks. Survivors are
+// appended (in any order: the visibility key carries the submission index).
+__global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
+    wait_previous_kernel();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < job.total_tri; base += stride) {
+        const uint32_t g = base + lane;
+        bool keep = false;
+        if (g < job.total_tri) {
+            const uint32_t si = seg_of_tri(job, g);
+            const DgSegDev& sg = job.segs[si];
+            const uint4 tp = __ldg(sg.tri_pos + (g - sg.tri_begin));
+            const float* mw = reinterpret_cast<const float*>(job.vrec + sg.vtx_begin) + 3;
+            const uint32_t m = __float_as_uint(__ldg(mw + 4ull * tp.x)) & __float_as_uint(__ldg(mw + 4ull * tp.y)) &
+                               __float_as_uint(__ldg(mw + 4ull * tp.z));
+            if (((m >> 8) & 0x3Du) == 0u) {
+                const float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
+                const V3 a = {pa.x, pa.y, pa.z}, b = {pb.x, pb.y, pb.z}, c = {pc.x, pc.y, pc.z};
+                // Triangle::calc_normal and get_center; skip when (cam - centre) . n <= 0
+                const V3 n = vcross(vsub(b, a), vsub(c, b));
+                const V3 zero = {0.0f, 0.0f, 0.0f};
+                const V3 ctr = vdiv(vadd(vadd(vadd(zero, a), b), c), 3.0f);
+                const DgFrameDev& fr = job.frames[sg.frame];
+                const V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
+                keep = !(vdot(vsub(cam, ctr), n) <= 0.0f);
+            }
+        }
+        const unsigned kb = __ballot_sync(FULL, keep);
+        if (kb) {
+            const int leader = __ffs(kb) - 1;
+            unsigned long long old = 0;
+            if ((int)lane == leader) old = atomicAdd(job.cnt + DG_CNT_SURV, (unsigned long long)__popc(kb));
+            old = __shfl_sync(FULL, old, leader);
+            if (keep) job.surv[old + __popc(kb & ((1u << lane) - 1u))] = g;
+        }
     }
 }
 
@@ -451,60 +629,84 @@ __device__ __forceinline__ void warp_flat_raster(const DgJobDev& job, const RTri
     }
 }
 
-// Kernels launched with programmatic dependent launch start before the previous
-// kernel of the stream has finished; this waits until it has completed and its
-// memory operations are visible.
-__device__ __forceinline__ void wait_previous_kernel() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Hands out n consecutive slots of counter c to every lane of the warp with one
+// atomic; returns this lane's first slot.
+__device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* c, uint32_t n) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    unsigned long long old = 0;
+    if (total != 0u) {
+        if (lane == 0u) old = atomicAdd(c, (unsigned long long)total);
+        old = __shfl_sync(FULL, old, 0);
+    }
+    return old + (incl - n);
+}
 
+// Setup pass over the cull survivors (dense, one per thread): near/far
+// clipping, triangle records, bounding boxes and edge functions; tiny
+// triangles are rasterized by their warp, the others are queued
+// (scene/mod.rs:1029-1063, canvas.rs:585-681).
 __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long ns64 = __ldcg(job.cnt + DG_CNT_SURV);
+    const uint32_t nsurv = (uint32_t)(ns64 < job.total_tri ? ns64 : job.total_tri);
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < job.total_tri; base += stride) {
-        const uint32_t g = base + lane;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nsurv; base += stride) {
+        const uint32_t i = base + lane;
         int nout = 0;
-        uint32_t si = 0, t = 0;
+        uint32_t g = 0, si = 0, t = 0, row0 = 0, nrows = 0;
         uint4 tp = make_uint4(0, 0, 0, 0);
         float4 r[3];
         bool clipped = false;
-        if (g < job.total_tri) {
+        if (i < nsurv) {
+            g = __ldcg(job.surv + i);
             si = seg_of_tri(job, g);
             const DgSegDev& sg = job.segs[si];
-            const DgFrameDev& fr = job.frames[sg.frame];
             t = g - sg.tri_begin;
             tp = __ldg(sg.tri_pos + t);
-            // The lateral trivial reject (Triangle::clip_against_planes, scene/mod.rs:59-66) and
-            // the back-face test (:1016-1027) are both pure predicates, so testing the cheap one
-            // first gives the same surviving set: the plane-sign masks of the vertex records
-            // reject most off-screen triangles before their positions are gathered.
             r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
             r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
             r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
             const uint32_t m = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
-            if (((m >> 8) & 0x3Cu) == 0u) {  // no lateral plane has all three f <= 0
+            if ((m & 0x3u) == 0x3u) {
+                nout = 1;  // inside near and far: the triangle passes unchanged
+            } else {
+                const DgFrameDev& fr = job.frames[sg.frame];
                 float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-                V3 a = {pa.x, pa.y, pa.z}, b = {pb.x, pb.y, pb.z}, c = {pc.x, pc.y, pc.z};
-                // back-face culling: Triangle::calc_normal, get_center; skip when (cam - centre) . n <= 0
-                V3 n = vcross(vsub(b, a), vsub(c, b));
-                V3 zero = {0.0f, 0.0f, 0.0f};
-                V3 ctr = vdiv(vadd(vadd(vadd(zero, a), b), c), 3.0f);
-                V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
-                if (!(vdot(vsub(cam, ctr), n) <= 0.0f)) {
-                    if ((m & 0x3u) == 0x3u) {
-                        nout = 1;  // inside near and far: the triangle passes unchanged
+                ClipProg P;
+                build_clip(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z}, P);
+                nout = P.nout;
+                clipped = true;
+                if (nout > 0 && P.nv > 3) {
+                    // rows of the light/halfway table for the new vertices
+                    nrows = (uint32_t)(P.nv - 3);
+                    const unsigned long long r0 = atomicAdd(job.cnt + DG_CNT_VROW, (unsigned long long)nrows);
+                    if (r0 + nrows <= job.vrow_extra) {
+                        row0 = (uint32_t)r0;
+                        clip_shade_rows(job, fr, P, row0);
                     } else {
-                        ClipProg P;
-                        build_clip(fr, a, b, c, P);
-                        nout = P.nout;
-                        clipped = true;
-                    }
-                    if (nout > 0) {  // its vertices need light/halfway vectors for shading
-                        const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
-                        for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+                        nrows = DG_NONE;  // no room: the resolve pass shades these pixels the long way
                     }
                 }
             }
+            if (nout > 0) {  // its vertices need light/halfway vectors for shading
+                const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
+                for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+            }
         }
+        // consecutive records for the clip outputs of each triangle
+        const unsigned long long rb = warp_alloc(job.cnt + DG_CNT_TREC, (uint32_t)nout);
+        uint32_t rbase = DG_NONE;
+        if (nout > 0 && nrows != DG_NONE && rb + (unsigned long long)nout <= job.trec_cap) rbase = (uint32_t)rb;
+        if (i < nsurv) job.rec_of[g] = rbase;
+
         for (int rr = 0;; rr++) {
             bool has = rr < nout;
             if (__ballot_sync(FULL, has) == 0u) break;
@@ -513,6 +715,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             uint32_t npx = 0;
             uint32_t nu = 0;     // work units to queue (0: not queued)
             uint64_t qpx = 0;    // bounding-box pixels of the queued triangle
+            bool inplace = false;
             tr.xlo = tr.xhi = tr.ylo = tr.yhi = 0;
             tr.frame = 0;
             if (has) {
@@ -520,6 +723,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                 const DgFrameDev& fr = job.frames[sg.frame];
                 tr.frame = sg.frame;
                 tr.seq = ((sg.seq_base + t) << 2) | (uint32_t)rr;
+                ClipProg P;
                 if (!clipped) {
                     tr.ax = r[0].x; tr.ay = r[0].y;
                     tr.bx = r[1].x; tr.by = r[1].y;
@@ -527,7 +731,6 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                     tr.da = r[0].z; tr.db = r[1].z; tr.dc = r[2].z;
                 } else {
                     float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-                    ClipProg P;
                     build_clip(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z}, P);
                     clip_output_tri(fr, P, rr, r, tr);
                 }
@@ -537,9 +740,17 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                     bbox_axis(tr.ax, tr.bx, tr.cx, fr.width, tr.xlo, tr.xhi);
                     bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
                     make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
+                    if (rbase != DG_NONE) {
+                        if (!clipped)
+                            write_record(job, sg, t, tp, e, r, rbase);
+                        else
+                            write_clip_record(job, sg, t, tp, e, tr, P, rr, row0, rbase + (uint32_t)rr);
+                    }
                     uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
                     if (px <= job.small_max_px) {
                         npx = (uint32_t)px;
+                    } else if (rbase == DG_NONE) {
+                        inplace = true;
                     } else {
                         qpx = px;
                         nu = (uint32_t)((px + DG_UNIT_PX - 1u) / DG_UNIT_PX);
@@ -547,61 +758,79 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                 }
             }
             // Queue this round's large triangles with one 64-bit atomic per warp: it hands out
-            // the record slots and their first work units together, so work-unit bases ascend
-            // with the slot (the queue pass binary-searches them).
+            // the queue records and their work items together; the warp then writes all its
+            // items, each lane taking every 32nd.
             const unsigned qmask = __ballot_sync(FULL, nu != 0u);
             if (qmask) {
-                uint32_t incl = nu;
+                const uint32_t ni = (nu + DG_ITEM_UNITS - 1u) / DG_ITEM_UNITS;
+                uint32_t incl = ni, uincl = nu;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    uint32_t v = __shfl_up_sync(FULL, incl, o);
-                    if (lane >= (uint32_t)o) incl += v;
+                    const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                    const uint32_t vu = __shfl_up_sync(FULL, uincl, o);
+                    if (lane >= (uint32_t)o) {
+                        incl += v;
+                        uincl += vu;
+                    }
                 }
-                const uint32_t total_units = __shfl_sync(FULL, incl, 31);
+                const uint32_t total_items = __shfl_sync(FULL, incl, 31);
+                const uint32_t total_units = __shfl_sync(FULL, uincl, 31);
                 const int leader = __ffs(qmask) - 1;
                 unsigned long long old = 0;
-                if ((int)lane == leader)
-                    old = atomicAdd(job.queue_counter,
-                                    ((unsigned long long)__popc(qmask) << DG_PACK_SHIFT) | total_units);
-                old = __shfl_sync(FULL, old, leader);
-                if (nu != 0u) {
-                    const uint64_t rec = (old >> DG_PACK_SHIFT) + __popc(qmask & ((1u << lane) - 1u));
-                    const uint64_t ubase = (old & ((1ull << DG_PACK_SHIFT) - 1ull)) + (incl - nu);
-                    // A record whose units would pass 2^32 is stored with no units (base
-                    // saturated, so bases stay ascending) and rasterized by this lane.
-                    const bool fits = ubase + nu <= 0xFFFFFFFFull;
-                    if (rec < job.queue_cap) {
-                        DgQueueRec q;
-                        q.ax = tr.ax; q.ay = tr.ay; q.bx = tr.bx; q.by = tr.by; q.cx = tr.cx; q.cy = tr.cy;
-                        q.da = tr.da; q.db = tr.db; q.dc = tr.dc;
-                        q.seq = tr.seq;
-                        q.frame = tr.frame;
-                        q.xlo = tr.xlo;
-                        q.ylo = tr.ylo;
-                        q.w = tr.xhi - tr.xlo + 1u;
-                        q.npx = (uint32_t)qpx;
-                        q.nunits = fits ? nu : 0u;
-                        job.queue[rec] = q;
-                        job.queue_base[rec] = fits ? (uint32_t)ubase : 0xFFFFFFFFu;
-                    }
-                    if (!(rec < job.queue_cap && fits)) {
-                        // queue full: this lane rasterizes the box itself
-                        atomicAdd(job.stats + 1, 1ull);
-                        const DgFrameDev& fr = job.frames[tr.frame];
-                        for (uint32_t y = tr.ylo; y <= tr.yhi; y++)
-                            for (uint32_t x = tr.xlo; x <= tr.xhi; x++)
-                                raster_pixel(e, tr.da, tr.db, tr.dc, tr.seq, x, y, fr);
-                    }
+                if ((int)lane == leader) {
+                    old = atomicAdd(job.cnt + DG_CNT_QUEUE,
+                                    ((unsigned long long)__popc(qmask) << DG_PACK_SHIFT) | total_items);
+                    atomicAdd(job.cnt + DG_CNT_UNITS, (unsigned long long)total_units);
                 }
+                old = __shfl_sync(FULL, old, leader);
+                const uint64_t rec = (old >> DG_PACK_SHIFT) + __popc(qmask & ((1u << lane) - 1u));
+                const uint64_t ibase = (old & ((1ull << DG_PACK_SHIFT) - 1ull)) + (incl - ni);
+                const bool fits = nu != 0u && rec < job.queue_cap && ibase + ni <= job.items_cap;
+                if (fits) {
+                    uint4* qd = reinterpret_cast<uint4*>(job.queue + rec);
+                    qd[0] = make_uint4(rbase + (uint32_t)rr, tr.seq, tr.frame, tr.xlo);
+                    qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, (uint32_t)qpx, nu);
+                } else if (nu != 0u) {
+                    inplace = true;  // queue full: this lane rasterizes the box itself
+                }
+                // items of all lanes: item j belongs to the first lane whose inclusive count exceeds it
+                const uint32_t excl = incl - ni;
+                for (uint32_t b0 = 0; b0 < total_items; b0 += 32u) {
+                    const uint32_t j = b0 + lane;
+                    int lo = 0, hi = 31;
+#pragma unroll
+                    for (int it = 0; it < 5; it++) {
+                        const int mid = (lo + hi) >> 1;
+                        if (__shfl_sync(FULL, incl, mid) > j)
+                            hi = mid;
+                        else
+                            lo = mid + 1;
+                    }
+                    const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, lo);
+                    const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, lo);
+                    const uint32_t oex = __shfl_sync(FULL, excl, lo);
+                    const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, lo) != 0u;
+                    const uint32_t k = j - oex;  // item index within its record
+                    // items of a lane that did not fit are marked empty (the slots are handed out)
+                    if (j < total_items && oib + k < job.items_cap)
+                        job.items[oib + k] = ofits ? make_uint2(orec, k * DG_ITEM_UNITS) : make_uint2(DG_NONE, 0u);
+                }
+            }
+            if (inplace) {  // this lane rasterizes the box itself
+                atomicAdd(job.cnt + DG_CNT_INPLACE, 1ull);
+                const DgFrameDev& fr = job.frames[tr.frame];
+                for (uint32_t y = tr.ylo; y <= tr.yhi; y++)
+                    for (uint32_t x = tr.xlo; x <= tr.xhi; x++)
+                        raster_pixel(e, tr.da, tr.db, tr.dc, tr.seq, x, y, fr);
             }
             warp_flat_raster(job, tr, e, npx);
         }
     }
 }
 
-// The raster queue: the bounding-box pixels of every queued triangle, numbered
-// row-major in units of DG_UNIT_PX and spread over all warps. A warp keeps its
-// current record (and edge constants) while consecutive units belong to it.
+// The raster queue: the bounding-box pixels of every queued triangle in
+// row-major units of DG_UNIT_PX (one pixel per lane), grouped into work items
+// of at most DG_ITEM_UNITS units that the warps take in a strided order.
 __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
@@ -616,39 +845,40 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
         if (((bits >> lane) & 1u) && (w << 5) + lane < job.total_vtx) shade_vertex(job, (w << 5) + lane);
         if (lane == 0) job.vmark[w] = 0u;
     }
-    const unsigned long long cnt = __ldcg(job.queue_counter);
-    const uint64_t nrec64 = cnt >> DG_PACK_SHIFT;
-    const uint32_t nrec = (uint32_t)(nrec64 < job.queue_cap ? nrec64 : job.queue_cap);
-    const uint64_t nu64 = cnt & ((1ull << DG_PACK_SHIFT) - 1ull);
-    const uint32_t nunits = (uint32_t)(nu64 < 0xFFFFFFFFull ? nu64 : 0xFFFFFFFFull);
-    if (nrec == 0) return;
-    uint32_t cur_base = 1u, cur_end = 0u;
-    DgQueueRec q;
-    EdgeSet e;
-    float rcp_w = 0.0f;
-    // Each warp takes a contiguous range of units, so consecutive units usually
-    // belong to the same record and the cached record and edge constants are reused.
-    const uint32_t per = (nunits + nwarps - 1u) / nwarps;
-    const uint32_t u0 = warp * per;
-    const uint32_t u1 = min(nunits, u0 + per);
-    for (uint32_t u = u0; u < u1; u++) {
-        if (!(u >= cur_base && u < cur_end)) {
-            uint32_t ri = last_le(nrec, u, [&](uint32_t i) { return __ldg(job.queue_base + i); });
-            q = job.queue[ri];
-            cur_base = __ldg(job.queue_base + ri);
-            cur_end = cur_base + q.nunits;
-            if (!(u >= cur_base && u < cur_end)) continue;  // unit of a record that did not fit the queue
-            make_edges(q.ax, q.ay, q.bx, q.by, q.cx, q.cy, e);
-            rcp_w = __frcp_rn((float)q.w);
-        }
-        const uint32_t k = (u - cur_base) * DG_UNIT_PX + lane;
-        if (k < q.npx) {
-            // k / w from a float reciprocal, corrected to the exact quotient
-            uint32_t yy = (uint32_t)__fmul_rz((float)k, rcp_w);
-            while ((uint64_t)yy * q.w > k) yy--;
-            while ((uint64_t)(yy + 1u) * q.w <= k) yy++;
-            const uint32_t xx = k - yy * q.w;
-            raster_pixel(e, q.da, q.db, q.dc, q.seq, q.xlo + xx, q.ylo + yy, job.frames[q.frame]);
+    const unsigned long long cnt = __ldcg(job.cnt + DG_CNT_QUEUE);
+    const uint64_t ni64 = cnt & ((1ull << DG_PACK_SHIFT) - 1ull);
+    const uint32_t nitems = (uint32_t)(ni64 < job.items_cap ? ni64 : job.items_cap);
+    for (uint32_t it = warp; it < nitems; it += nwarps) {
+        const uint2 item = __ldcg(job.items + it);
+        if (item.x >= job.queue_cap) continue;  // an item of a triangle that did not fit the queue
+        const uint4* qs = reinterpret_cast<const uint4*>(job.queue + item.x);
+        const uint4 q0 = __ldcg(qs), q1 = __ldcg(qs + 1);
+        const DgTriRec* R = job.trec + q0.x;
+        EdgeSet e;
+        load_edges(R, e);
+        const float4 dd = __ldg(reinterpret_cast<const float4*>(R) + 4);
+        const uint32_t seq = q0.y;
+        const DgFrameDev& fr = job.frames[q0.z];
+        const float clear_depth = fr.clear_depth;
+        unsigned long long* vis = reinterpret_cast<unsigned long long*>(fr.vis);
+        const uint32_t width = fr.width;
+        const uint32_t xlo = q0.w, ylo = q1.x, w = q1.y, npx = q1.z;
+        const float rcp_w = __frcp_rn((float)w);
+        const uint32_t u_end = min(q1.w, item.y + DG_ITEM_UNITS);
+        for (uint32_t u = item.y; u < u_end; u++) {
+            const uint32_t k = u * DG_UNIT_PX + lane;
+            if (k < npx) {
+                // k / w from a float reciprocal, corrected to the exact quotient
+                uint32_t yy = (uint32_t)__fmul_rz((float)k, rcp_w);
+                while ((uint64_t)yy * w > k) yy--;
+                while ((uint64_t)(yy + 1u) * w <= k) yy++;
+                const uint32_t x = xlo + (k - yy * w), y = ylo + yy;
+                float al, be, ga;
+                if (covered(e, (float)x, (float)y, al, be, ga)) {
+                    const float depth = interp(al, be, ga, dd.x, dd.y, dd.z);
+                    if (depth < clear_depth) atomicMin(vis + (uint64_t)y * width + x, depth_key(depth, seq));
+                }
+            }
         }
     }
 }
@@ -657,22 +887,148 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
 // reference's wrapping usize arithmetic; false where the reference's slice
 // index would panic.
 __device__ __forceinline__ bool tex_rgb(const DgTexDev& tx, float u, float v, uint32_t& rgb) {
-    uint64_t ui = as_usize(floorf(fM(u, fS(tx.fw, 1.0f))));
-    uint64_t vi = (uint64_t)tx.height - 1ull - as_usize(floorf(fM(v, fS(tx.fh, 1.0f))));
-    uint64_t off = (vi * (uint64_t)tx.width + ui) * (uint64_t)tx.comps;
+    const float fu = floorf(fM(u, fS(tx.fw, 1.0f)));
+    const float fv = floorf(fM(v, fS(tx.fh, 1.0f)));
+    uint64_t off;
+    if (tx.small != 0u && fu >= 0.0f && fu < tx.fw && fv >= 0.0f && fv < tx.fh) {
+        // both indices inside the map: the wrapping usize arithmetic below reduces
+        // to this 32-bit one (the offset is below len < 2^32)
+        off = ((tx.height - 1u - (uint32_t)fv) * tx.width + (uint32_t)fu) * tx.comps;
+    } else {
+        const uint64_t ui = as_usize(fu);
+        const uint64_t vi = (uint64_t)tx.height - 1ull - as_usize(fv);
+        off = (vi * (uint64_t)tx.width + ui) * (uint64_t)tx.comps;
+    }
     if (tx.len < 3ull || off > tx.len - 3ull) return false;
-    uint64_t w = off >> 2;
-    uint32_t lo = __ldg(tx.words + w), hi = __ldg(tx.words + w + 1);
-    rgb = __funnelshift_r(lo, hi, (uint32_t)(off & 3ull) * 8u);
+    const uint64_t w = off >> 2;
+    const uint32_t sh = (uint32_t)(off & 3ull) * 8u;
+    const uint32_t lo = __ldg(tx.words + w);
+    // the three bytes span two words only when the offset is not word aligned
+    rgb = sh <= 8u ? (lo >> sh) : __funnelshift_r(lo, __ldg(tx.words + w + 1), sh);
     return true;
 }
 
-// Shades the winning fragment of pixel (x, y): canvas.rs:682-741.
-__device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint32_t seq, uint32_t x, uint32_t y,
-                                const float* inv255, float& depth_out, int& errc) {
+// A triangle's material as the shading formula uses it.
+struct MatVals {
+    V3 ka, kd, ks;
+    uint32_t map_ka, map_kd;
+};
+
+// Texture descriptors the shade pass keeps in shared memory (the rest are read
+// from the job's table).
+#define DG_SMEM_TEX 32u
+
+// Shading of canvas.rs:713-741 from the interpolated texture coordinates,
+// normal and per-light vectors: lv(l, lt, h) gives the interpolated light and
+// halfway vectors of light l.
+template <class LV>
+__device__ __forceinline__ uint32_t shade_colour(const DgJobDev& job, const DgTexDev* stex, const DgFrameDev& fr,
+                                                 const MatVals& m, float pu, float pv, V3 pn, const float* inv255,
+                                                 int& errc, LV lv) {
+    const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
+    const DgTexDev& tkd = m.map_kd < nst ? stex[m.map_kd] : job.tex[m.map_kd];
+    const DgTexDev& tka = m.map_ka < nst ? stex[m.map_ka] : job.tex[m.map_ka];
+    uint32_t kd_rgb = 0, ka_rgb = 0;
+    if (!tex_rgb(tkd, pu, pv, kd_rgb)) {
+        errc = DG_E_TEXTURE_RANGE;
+        return 0u;
+    }
+    if (m.map_ka == m.map_kd) {
+        ka_rgb = kd_rgb;  // the same map at the same coordinates
+    } else if (!tex_rgb(tka, pu, pv, ka_rgb)) {
+        errc = DG_E_TEXTURE_RANGE;
+        return 0u;
+    }
+    // Pixel::normalized_as_vec3 (canvas.rs:81-87): byte / 255.0, looked up in a
+    // table of the 256 correctly rounded quotients
+    const V3 diffuse = {inv255[kd_rgb & 0xFFu], inv255[(kd_rgb >> 8) & 0xFFu], inv255[(kd_rgb >> 16) & 0xFFu]};
+    const V3 ambient = {inv255[ka_rgb & 0xFFu], inv255[(ka_rgb >> 8) & 0xFFu], inv255[(ka_rgb >> 16) & 0xFFu]};
+    const V3 c_l = m.ks;
+    const V3 c_r = {fM(diffuse.x, m.kd.x), fM(diffuse.y, m.kd.y), fM(diffuse.z, m.kd.z)};
+    const V3 c_a = {fM(ambient.x, m.ka.x), fM(ambient.y, m.ka.y), fM(ambient.z, m.ka.z)};
+    const uint32_t nl = fr.nlights;
+    // The per-light H.N dots are taken in the first loop (one read of each light's
+    // vectors) and used in the second, in the reference's order of operations.
+    float hn[DG_MAXL];
+    V3 inner = c_a;
+#pragma unroll
+    for (uint32_t l = 0; l < DG_MAXL; l++) {
+        if (l < nl) {
+            V3 lt, h;
+            lv(l, lt, h);
+            const float ln = vdot(lt, pn);
+            const float mx = ln > 0.0f ? ln : 0.0f;  // 0.0_f32.max(x): NaN -> 0
+            inner = vadd(inner, vmul(c_l, fS(1.0f, mx)));
+            hn[l] = vdot(h, pn);
+        }
+    }
+    V3 col = {fM(c_r.x, inner.x), fM(c_r.y, inner.y), fM(c_r.z, inner.z)};
+    const int32_t ex = fr.exponent;
+#pragma unroll
+    for (uint32_t l = 0; l < DG_MAXL; l++)
+        if (l < nl) col = vadd(col, vmul(c_l, powi(hn[l], ex)));
+    // Pixel::from_normalized_vec3 (canvas.rs:89-92), stored as b,g,r,255
+    const V3 sc = vmul(col, 255.0f);
+    const uint32_t R = as_u8(sc.x), G = as_u8(sc.y), B = as_u8(sc.z);
+    return B | (G << 8) | (R << 16) | (255u << 24);
+}
+
+// Row `row` of the light/halfway table for light l: (lt.x, lt.y, lt.z, h.x), (h.y, h.z, -, -).
+__device__ __forceinline__ const float4* shade_row(const DgJobDev& job, uint32_t row, uint32_t l) {
+    return job.vshade + ((uint64_t)row * job.shade_stride + l) * 2;
+}
+
+// Shades the winning fragment of pixel (x, y) from its triangle record:
+// canvas.rs:682-741.
+__device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const DgFrameDev& fr, const DgTriRec* R,
+                                                      uint32_t x, uint32_t y, const float* inv255,
+                                                      const DgTexDev* stex, float& depth_out, int& errc) {
+    errc = DG_OK;
+    EdgeSet e;
+    load_edges(R, e);
+    const float4* q = reinterpret_cast<const float4*>(R);
+    const float4 dd = __ldg(q + 4), fu = __ldg(q + 5), fv = __ldg(q + 6);
+    const float4 fx = __ldg(q + 7), fy = __ldg(q + 8), fz = __ldg(q + 9);
+    const uint4 rows = __ldg(reinterpret_cast<const uint4*>(R) + 10);
+    const uint4 last = __ldg(reinterpret_cast<const uint4*>(R) + 11);
+    const float xf = (float)x, yf = (float)y;
+    const float al = fD(edge_eval(e, 0, xf, yf), e.den[0]);
+    const float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
+    const float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
+    depth_out = interp(al, be, ga, dd.x, dd.y, dd.z);
+    const float pu = interp(al, be, ga, fu.x, fu.y, fu.z);
+    const float pv = interp(al, be, ga, fv.x, fv.y, fv.z);
+    const V3 pn = {interp(al, be, ga, fx.x, fx.y, fx.z), interp(al, be, ga, fy.x, fy.y, fy.z),
+                   interp(al, be, ga, fz.x, fz.y, fz.z)};
+    MatVals m;
+    m.ka = V3{dd.w, fu.w, fv.w};
+    m.kd = V3{fx.w, fy.w, fz.w};
+    m.ks = V3{__uint_as_float(rows.w), __uint_as_float(last.x), __uint_as_float(last.y)};
+    m.map_ka = last.z;
+    m.map_kd = last.w;
+    auto lv = [&](uint32_t l, V3& lt, V3& h) {
+        const float4* pa = shade_row(job, rows.x, l);
+        const float4* pb = shade_row(job, rows.y, l);
+        const float4* pc = shade_row(job, rows.z, l);
+        const float4 a = __ldg(pa), b = __ldg(pb), c = __ldg(pc);
+        const float4 a1 = __ldg(pa + 1), b1 = __ldg(pb + 1), c1 = __ldg(pc + 1);
+        lt = V3{interp(al, be, ga, a.x, b.x, c.x), interp(al, be, ga, a.y, b.y, c.y),
+                interp(al, be, ga, a.z, b.z, c.z)};
+        h = V3{interp(al, be, ga, a.w, b.w, c.w), interp(al, be, ga, a1.x, b1.x, c1.x),
+               interp(al, be, ga, a1.y, b1.y, c1.y)};
+    };
+    return shade_colour(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
+}
+
+// Shades the winning fragment of pixel (x, y) from its key alone (the triangle
+// has no record: the record buffers were full): the triangle is set up and
+// clipped again here.
+__device__ __noinline__ uint32_t shade_without_record(const DgJobDev& job, const DgFrameDev& fr, uint32_t seq,
+                                                      uint32_t x, uint32_t y, const float* inv255,
+                                                      const DgTexDev* stex, float& depth_out, int& errc) {
     errc = DG_OK;
     const uint32_t tl = seq >> 2, o = seq & 3u;
-    uint32_t si =
+    const uint32_t si =
         fr.seg_begin + last_le(fr.seg_count, tl, [&](uint32_t i) { return job.segs[fr.seg_begin + i].seq_base; });
     const DgSegDev& sg = job.segs[si];
     const uint32_t t = tl - sg.seq_base;
@@ -710,8 +1066,10 @@ __device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint3
     }
     EdgeSet e;
     make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
-    float al = 0.0f, be = 0.0f, ga = 0.0f;
-    covered(e, (float)x, (float)y, al, be, ga);
+    const float xf = (float)x, yf = (float)y;
+    const float al = fD(edge_eval(e, 0, xf, yf), e.den[0]);
+    const float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
+    const float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
     depth_out = interp(al, be, ga, tr.da, tr.db, tr.dc);
 
     // per-vertex field values of the output triangle
@@ -734,82 +1092,161 @@ __device__ uint32_t shade_pixel(const DgJobDev& job, const DgFrameDev& fr, uint3
     const float pv = field(uv[0].y, uv[1].y, uv[2].y);
     const V3 pn = {field(nr[0].x, nr[1].x, nr[2].x), field(nr[0].y, nr[1].y, nr[2].y),
                    field(nr[0].z, nr[1].z, nr[2].z)};
-    const DgMatDev& mat = sg.mats[tp.w];
-    uint32_t kd_rgb = 0, ka_rgb = 0;
-    if (!tex_rgb(job.tex[mat.map_kd], pu, pv, kd_rgb) || !tex_rgb(job.tex[mat.map_ka], pu, pv, ka_rgb)) {
-        errc = DG_E_TEXTURE_RANGE;
+    if (tp.w >= sg.nmats) {
+        errc = DG_E_CUDA;
         return 0u;
     }
-    // Pixel::normalized_as_vec3 (canvas.rs:81-87): byte / 255.0, looked up in a
-    // table of the 256 correctly rounded quotients
-    const V3 diffuse = {inv255[kd_rgb & 0xFFu], inv255[(kd_rgb >> 8) & 0xFFu], inv255[(kd_rgb >> 16) & 0xFFu]};
-    const V3 ambient = {inv255[ka_rgb & 0xFFu], inv255[(ka_rgb >> 8) & 0xFFu], inv255[(ka_rgb >> 16) & 0xFFu]};
-    const V3 c_l = {mat.ks[0], mat.ks[1], mat.ks[2]};
-    const V3 c_r = {fM(diffuse.x, mat.kd[0]), fM(diffuse.y, mat.kd[1]), fM(diffuse.z, mat.kd[2])};
-    const V3 c_a = {fM(ambient.x, mat.ka[0]), fM(ambient.y, mat.ka[1]), fM(ambient.z, mat.ka[2])};
-    V3 inner = c_a;
-    for (uint32_t l = 0; l < fr.nlights; l++) {
-        float4 s0[3];
-        for (int k = 0; k < 3; k++) s0[k] = __ldg(job.vshade + ((uint64_t)(sg.vtx_begin + vi[k]) * job.shade_stride + l) * 2);
-        V3 pl = {field(s0[0].x, s0[1].x, s0[2].x), field(s0[0].y, s0[1].y, s0[2].y), field(s0[0].z, s0[1].z, s0[2].z)};
-        float ln = vdot(pl, pn);
-        float mx = ln > 0.0f ? ln : 0.0f;  // 0.0_f32.max(x): NaN -> 0
-        inner = vadd(inner, vmul(c_l, fS(1.0f, mx)));
-    }
-    V3 col = {fM(c_r.x, inner.x), fM(c_r.y, inner.y), fM(c_r.z, inner.z)};
-    for (uint32_t l = 0; l < fr.nlights; l++) {
-        float4 s0[3], s1[3];
-        for (int k = 0; k < 3; k++) {
-            const float4* src = job.vshade + ((uint64_t)(sg.vtx_begin + vi[k]) * job.shade_stride + l) * 2;
-            s0[k] = __ldg(src);
-            s1[k] = __ldg(src + 1);
-        }
-        V3 ph = {field(s0[0].w, s0[1].w, s0[2].w), field(s1[0].x, s1[1].x, s1[2].x), field(s1[0].y, s1[1].y, s1[2].y)};
-        col = vadd(col, vmul(c_l, powi(vdot(ph, pn), fr.exponent)));
-    }
-    // Pixel::from_normalized_vec3 (canvas.rs:89-92), stored as b,g,r,255
-    V3 sc = vmul(col, 255.0f);
-    uint32_t R = as_u8(sc.x), G = as_u8(sc.y), B = as_u8(sc.z);
-    return B | (G << 8) | (R << 16) | (255u << 24);
+    const DgMatDev& md = sg.mats[tp.w];
+    MatVals m;
+    m.ka = V3{md.ka[0], md.ka[1], md.ka[2]};
+    m.kd = V3{md.kd[0], md.kd[1], md.kd[2]};
+    m.ks = V3{md.ks[0], md.ks[1], md.ks[2]};
+    m.map_ka = md.map_ka;
+    m.map_kd = md.map_kd;
+    // Clip vertices' light/halfway vectors come from the input vertices' rows
+    // through the clip program (clip_shade_rows computes the same values).
+    auto comp = [&](uint32_t l, int c) {
+        auto at = [&](int k) {
+            return __ldg(reinterpret_cast<const float*>(shade_row(job, sg.vtx_begin + vi[k], l)) + c);
+        };
+        return field(at(0), at(1), at(2));
+    };
+    auto lv = [&](uint32_t l, V3& lt, V3& h) {
+        lt = V3{comp(l, 0), comp(l, 1), comp(l, 2)};
+        h = V3{comp(l, 3), comp(l, 4), comp(l, 5)};
+    };
+    return shade_colour(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
 }
 
+// Shade-list entry: x = job-wide pixel index, with DG_SHADE_KEY set when y holds
+// the key's low word (no triangle record) instead of the record index.
+#define DG_SHADE_KEY 0x80000000u
+
+// Resolve, pass 1 (one 32 x 32 tile per CTA, four rows per thread): an empty
+// pixel gets the clear colour and depth; a covered one has its key reset for
+// the next frame and is appended to the shade list with its triangle record
+// (one atomic per tile).
 __global__ void __launch_bounds__(256) k_resolve(const DgJobDev job) {
-    __shared__ float inv255[256];
-    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);  // independent of the previous kernel
+    __shared__ __align__(8) uint32_t sh[12];
     wait_previous_kernel();
-    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t tile = blockIdx.x;
     const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
     const DgFrameDev& fr = job.frames[fi];
     const uint32_t lt = tile - fr.tile_begin;
     const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
-    const uint32_t x = tx * DG_TILE_W + (threadIdx.x & (DG_TILE_W - 1u));
-    const uint32_t y = ty * DG_TILE_H + threadIdx.x / DG_TILE_W;
-    const bool in = x < fr.width && y < fr.height;
-    bool hit = false;
-    if (in) {
-        const uint64_t i = (uint64_t)y * fr.width + x;
-        const uint64_t ci = (uint64_t)(fr.height - 1u - y) * fr.width + x;
-        const uint64_t key = __ldcg(reinterpret_cast<const unsigned long long*>(fr.vis) + i);
-        if (key == DG_VIS_EMPTY) {
+    const uint32_t x = tx * DG_TILE_W + lane;
+    const uint32_t y0 = ty * DG_TILE_H + (threadIdx.x >> 5);
+    const uint32_t W = fr.width, H = fr.height;
+    constexpr int R = DG_TILE_H / 8;
+    uint64_t key[R];
+#pragma unroll
+    for (int j = 0; j < R; j++) {  // all loads first: four keys in flight per thread
+        const uint32_t y = y0 + 8u * j;
+        key[j] = (x < W && y < H) ? __ldcg(reinterpret_cast<const unsigned long long*>(fr.vis) + (uint64_t)y * W + x)
+                                  : DG_VIS_EMPTY - 1ull;  // outside the canvas
+    }
+    uint32_t val[R];
+    uint32_t nhit = 0;
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        const uint32_t y = y0 + 8u * j;
+        const uint64_t i = (uint64_t)y * W + x;
+        val[j] = DG_NONE;
+        if (key[j] == DG_VIS_EMPTY) {
             fr.depth[i] = fr.clear_depth;
-            fr.colour[ci] = AZUL_BB;
-        } else {
-            hit = true;
+            fr.colour[(uint64_t)(H - 1u - y) * W + x] = AZUL_BB;
+        } else if (key[j] < DG_VIS_EMPTY - 1ull) {
             fr.vis[i] = DG_VIS_EMPTY;
-            float d = 0.0f;
-            int errc;
-            uint32_t c = shade_pixel(job, fr, (uint32_t)key, x, y, inv255, d, errc);
-            if (errc != DG_OK) {
-                atomicOr(job.err, 1u << errc);
-                c = AZUL_BB;
-            }
-            fr.depth[i] = d;
-            fr.colour[ci] = c;
+            nhit++;
+            // the triangle record of the key: segment of the submission index, then rec_of
+            const uint32_t seq = (uint32_t)key[j];
+            const uint32_t tl = seq >> 2;
+            const uint32_t si = fr.seg_begin + last_le(fr.seg_count, tl, [&](uint32_t k) {
+                                    return job.segs[fr.seg_begin + k].seq_base;
+                                });
+            const DgSegDev& sg = job.segs[si];
+            const uint32_t t = tl - sg.seq_base;
+            if (t < sg.ntri) val[j] = __ldg(job.rec_of + sg.tri_begin + t);
         }
     }
-    unsigned m = __ballot_sync(FULL, hit);
-    if ((threadIdx.x & 31u) == 0u && m) atomicAdd(job.stats, (unsigned long long)__popc(m));
+    // one atomic per tile for the shade-list slots of its covered pixels
+    const uint32_t wid = threadIdx.x >> 5;
+    uint32_t incl = nhit;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31u) sh[wid] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t w = 0; w < 8u; w++) {
+            const uint32_t k = sh[w];
+            sh[w] = run;
+            run += k;
+        }
+        *reinterpret_cast<unsigned long long*>(sh + 10) =
+            run ? atomicAdd(job.cnt + DG_CNT_COVERED, (unsigned long long)run) : 0ull;
+    }
+    __syncthreads();
+    unsigned long long slot = *reinterpret_cast<unsigned long long*>(sh + 10) + sh[wid] + (incl - nhit);
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        if (key[j] < DG_VIS_EMPTY - 1ull) {
+            const uint32_t y = y0 + 8u * j;
+            const uint32_t p = fr.pix_begin + (uint32_t)((uint64_t)y * W + x);
+            const uint32_t seq = (uint32_t)key[j];
+            uint2 ent;
+            if (val[j] != DG_NONE && (uint64_t)val[j] + (seq & 3u) < job.trec_cap)
+                ent = make_uint2(p, val[j] + (seq & 3u));
+            else
+                ent = make_uint2(p | DG_SHADE_KEY, seq);
+            if (slot < job.total_px) job.shade_list[slot] = ent;
+            slot++;
+        }
+    }
+}
+
+// Resolve, pass 2: the winning fragment of every covered pixel is shaded once
+// (canvas.rs:682-741) and its colour (row H-1-y) and depth (y*W+x) are written
+// (canvas.rs:923-930). Dense over the shade list.
+__global__ void __launch_bounds__(256, 4) k_shade(const DgJobDev job) {
+    __shared__ float inv255[256];
+    __shared__ DgTexDev stex[DG_SMEM_TEX];
+    // independent of the previous kernel: the quotient table and the texture descriptors
+    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
+    const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
+    for (uint32_t i = threadIdx.x; i < nst * 3u; i += blockDim.x)
+        reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
+    wait_previous_kernel();
+    __syncthreads();
+    const unsigned long long n64 = __ldcg(job.cnt + DG_CNT_COVERED);
+    const uint32_t n = (uint32_t)(n64 < job.total_px ? n64 : job.total_px);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const uint2 ent = __ldcg(job.shade_list + k);
+        const uint32_t p = ent.x & ~DG_SHADE_KEY;
+        const uint32_t fi = last_le(job.nframes, p, [&](uint32_t i) { return job.frames[i].pix_begin; });
+        const DgFrameDev& fr = job.frames[fi];
+        const uint32_t local = p - fr.pix_begin;
+        const uint32_t y = local / fr.width, x = local - y * fr.width;
+        float d = 0.0f;
+        int errc;
+        uint32_t c;
+        if (ent.x & DG_SHADE_KEY)
+            c = shade_without_record(job, fr, ent.y, x, y, inv255, stex, d, errc);
+        else
+            c = shade_from_record(job, fr, job.trec + ent.y, x, y, inv255, stex, d, errc);
+        if (errc != DG_OK) c = AZUL_BB;
+        // one error-word update per warp (every pixel of a bad job may fail)
+        const unsigned act = __activemask();
+        const uint32_t bits = __reduce_or_sync(act, errc != DG_OK ? 1u << errc : 0u);
+        if (bits != 0u && (threadIdx.x & 31u) == (uint32_t)(__ffs(act) - 1)) atomicOr(job.err, bits);
+        fr.depth[local] = d;
+        fr.colour[(uint64_t)(fr.height - 1u - y) * fr.width + x] = c;
+    }
 }
 
 __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, float dv, int fc, int fd) {
@@ -830,14 +1267,6 @@ inline unsigned grid_for(uint64_t n, unsigned cap) {
     return (unsigned)(g < cap ? g : cap);
 }
 
-}  // namespace
-
-cudaError_t dg_launch_vertex(const DgJobDev& job, cudaStream_t s) {
-    if (job.total_vtx == 0) return cudaSuccess;
-    k_vertex<<<grid_for(job.total_vtx, 1u << 20), 256, 0, s>>>(job);
-    return cudaGetLastError();
-}
-
 // Programmatic dependent launch: the kernel may be scheduled while the previous
 // kernel of the stream drains; it calls wait_previous_kernel() before reading
 // anything that kernel wrote.
@@ -856,19 +1285,41 @@ cudaError_t launch_dependent(void (*kern)(DgJobDev), unsigned grid, unsigned blo
     return cudaLaunchKernelEx(&cfg, kern, job);
 }
 
-cudaError_t dg_launch_setup_raster(const DgJobDev& job, unsigned max_blocks, cudaStream_t s) {
-    if (job.total_tri == 0) return cudaSuccess;
-    return launch_dependent(k_setup_raster, grid_for(job.total_tri, max_blocks < 1u ? 1u : max_blocks), 256, job, s);
-}
+}  // namespace
 
-cudaError_t dg_launch_queue_raster(const DgJobDev& job, unsigned blocks, cudaStream_t s) {
-    if (job.total_tri == 0) return cudaSuccess;
-    return launch_dependent(k_queue_raster, blocks < 1u ? 1u : blocks, 256, job, s);
-}
-
-cudaError_t dg_launch_resolve(const DgJobDev& job, cudaStream_t s) {
-    if (job.total_tiles == 0) return cudaSuccess;
-    return launch_dependent(k_resolve, job.total_tiles, 256, job, s);
+cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev) {
+    cudaError_t e;
+    auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
+    if ((e = mark(0)) != cudaSuccess) return e;
+    if (job.total_vtx) {
+        k_vertex<<<grid_for(job.total_vtx, 1u << 20), 256, 0, s>>>(job);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = mark(1)) != cudaSuccess) return e;
+    if (job.total_tri) {
+        const unsigned cb = cfg.cull_blocks < 1u ? 1u : cfg.cull_blocks;
+        if ((e = launch_dependent(k_cull, grid_for(job.total_tri, cb), 256, job, s)) != cudaSuccess) return e;
+    }
+    if ((e = mark(2)) != cudaSuccess) return e;
+    if (job.total_tri) {
+        const unsigned sb = cfg.setup_blocks < 1u ? 1u : cfg.setup_blocks;
+        if ((e = launch_dependent(k_setup_raster, grid_for(job.total_tri, sb), 256, job, s)) != cudaSuccess) return e;
+    }
+    if ((e = mark(3)) != cudaSuccess) return e;
+    if (job.total_tri) {
+        const unsigned qb = cfg.queue_blocks < 1u ? 1u : cfg.queue_blocks;
+        if ((e = launch_dependent(k_queue_raster, qb, 256, job, s)) != cudaSuccess) return e;
+    }
+    if ((e = mark(4)) != cudaSuccess) return e;
+    if (job.total_tiles) {
+        if ((e = launch_dependent(k_resolve, job.total_tiles, 256, job, s)) != cudaSuccess) return e;
+    }
+    if ((e = mark(5)) != cudaSuccess) return e;
+    if (job.total_px) {
+        const unsigned hb = cfg.shade_blocks < 1u ? 1u : cfg.shade_blocks;
+        if ((e = launch_dependent(k_shade, grid_for(job.total_px, hb), 256, job, s)) != cudaSuccess) return e;
+    }
+    return mark(6);
 }
 
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,

@@ -30,14 +30,20 @@ struct NoallocDesc {  // the job descriptor the kernels read
     DgMatDev mats[DG_NOALLOC_MAX_MATERIALS];
 };
 constexpr size_t kOffDesc = 0;
+constexpr uint32_t kVrowExtra = 4096;  // light/halfway rows for clip vertices
+constexpr uint32_t kTrecCap = DG_NOALLOC_MAX_TRIANGLES + 4096;  // triangle records
 constexpr size_t kOffVrec = align_up(kOffDesc + sizeof(NoallocDesc));
 constexpr size_t kOffVshade = align_up(kOffVrec + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(float4));
-constexpr size_t kOffVmark =
-    align_up(kOffVshade + (size_t)DG_NOALLOC_MAX_VERTICES * DG_NOALLOC_MAX_LIGHTS * 2 * sizeof(float4));
+constexpr size_t kOffVmark = align_up(kOffVshade + (size_t)(DG_NOALLOC_MAX_VERTICES + kVrowExtra) *
+                                                       DG_NOALLOC_MAX_LIGHTS * 2 * sizeof(float4));
 constexpr size_t kOffQueue = align_up(kOffVmark + (size_t)(DG_NOALLOC_MAX_VERTICES / 32) * sizeof(uint32_t));
 constexpr size_t kOffQbase = align_up(kOffQueue + (size_t)kQueueCap * sizeof(DgQueueRec));
-constexpr size_t kOffCounters = align_up(kOffQbase + (size_t)kQueueCap * sizeof(uint32_t));
-constexpr size_t kOffErr = align_up(kOffCounters + 4 * sizeof(unsigned long long));
+constexpr size_t kOffSurv = align_up(kOffQbase + (size_t)dg_items_cap(kQueueCap) * sizeof(uint2));
+constexpr size_t kOffRecOf = align_up(kOffSurv + (size_t)DG_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t));
+constexpr size_t kOffTrec = align_up(kOffRecOf + (size_t)DG_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t));
+constexpr size_t kOffShade = align_up(kOffTrec + (size_t)kTrecCap * sizeof(DgTriRec));
+constexpr size_t kOffCounters = align_up(kOffShade + (size_t)DG_NOALLOC_MAX_PIXELS * sizeof(uint2));
+constexpr size_t kOffErr = align_up(kOffCounters + DG_NCOUNTERS * sizeof(unsigned long long));
 constexpr size_t kOffWhite = align_up(kOffErr + sizeof(uint32_t));
 constexpr size_t kOffVis = align_up(kOffWhite + 8);
 constexpr size_t kScratchBytes = align_up(kOffVis + (size_t)DG_NOALLOC_MAX_PIXELS * sizeof(uint64_t));
@@ -135,6 +141,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     f.seg_count = 1;
     f.tile_begin = 0;
     f.tiles_x = (p->canvas_width + DG_TILE_W - 1) / DG_TILE_W;
+    f.pix_begin = 0;
     const uint32_t tiles = f.tiles_x * ((p->canvas_height + DG_TILE_H - 1) / DG_TILE_H);
 
     DgSegDev& sg = d.seg;
@@ -159,6 +166,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     d.tex[0].width = d.tex[0].height = 1;
     d.tex[0].comps = 3;
     d.tex[0].fw = d.tex[0].fh = 1.0f;
+    d.tex[0].small = 1;
     for (uint32_t i = 0; i < ntex; i++) {
         d.tex[i + 1].words = static_cast<const uint32_t*>(texmaps[i].bytes);
         d.tex[i + 1].len = texmaps[i].len;
@@ -167,6 +175,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
         d.tex[i + 1].comps = texmaps[i].components;
         d.tex[i + 1].fw = (float)texmaps[i].width;
         d.tex[i + 1].fh = (float)texmaps[i].height;
+        d.tex[i + 1].small = dg_tex_small(texmaps[i].len, texmaps[i].width, texmaps[i].height);
     }
     for (uint32_t i = 0; i < nmat; i++) {
         for (int k = 0; k < 3; k++) {
@@ -190,14 +199,22 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.shade_stride = p->nlights;
     job.vrec = reinterpret_cast<float4*>(base + kOffVrec);
     job.vshade = reinterpret_cast<float4*>(base + kOffVshade);
+    job.vrow_extra = kVrowExtra;
     job.vmark = reinterpret_cast<uint32_t*>(base + kOffVmark);
+    job.surv = reinterpret_cast<uint32_t*>(base + kOffSurv);
+    job.rec_of = reinterpret_cast<uint32_t*>(base + kOffRecOf);
+    job.trec = reinterpret_cast<DgTriRec*>(base + kOffTrec);
+    job.trec_cap = kTrecCap;
     job.queue = reinterpret_cast<DgQueueRec*>(base + kOffQueue);
-    job.queue_base = reinterpret_cast<uint32_t*>(base + kOffQbase);
+    job.items = reinterpret_cast<uint2*>(base + kOffQbase);
+    job.items_cap = (uint32_t)dg_items_cap(kQueueCap);
     job.queue_cap = kQueueCap;
     job.small_max_px = DG_SMALL_MAX_PX;
-    job.queue_counter = reinterpret_cast<unsigned long long*>(base + kOffCounters);
-    job.stats = job.queue_counter + 1;
+    job.cnt = reinterpret_cast<unsigned long long*>(base + kOffCounters);
+    job.total_px = (uint32_t)npx;
+    job.shade_list = reinterpret_cast<uint2*>(base + kOffShade);
     job.tex = reinterpret_cast<const DgTexDev*>(base + kOffDesc + offsetof(NoallocDesc, tex));
+    job.ntex = ntex + 1;
     job.err = reinterpret_cast<uint32_t*>(base + kOffErr);
 
     int dev = 0, nsm = 0;
@@ -207,16 +224,18 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     // Pageable source: the copy has taken the descriptor when cudaMemcpyAsync returns.
     NA_CUDA(cudaMemcpyAsync(base + kOffDesc, &d, sizeof(d), cudaMemcpyHostToDevice, s));
     // Reset what the previous call left behind.
-    NA_CUDA(cudaMemsetAsync(base + kOffCounters, 0, 4 * sizeof(unsigned long long), s));
+    NA_CUDA(cudaMemsetAsync(base + kOffCounters, 0, DG_NCOUNTERS * sizeof(unsigned long long), s));
     NA_CUDA(cudaMemsetAsync(base + kOffErr, 0, sizeof(uint32_t), s));
     NA_CUDA(cudaMemsetAsync(base + kOffVmark, 0, (size_t)(DG_NOALLOC_MAX_VERTICES / 32) * sizeof(uint32_t), s));
     NA_CUDA(cudaMemsetAsync(base + kOffWhite, 0xFF, 8, s));
     NA_CUDA(dg_launch_vis_reset(reinterpret_cast<uint64_t*>(base + kOffVis), npx, s));
 
-    NA_CUDA(dg_launch_vertex(job, s));
-    NA_CUDA(dg_launch_setup_raster(job, (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM, s));
-    NA_CUDA(dg_launch_queue_raster(job, (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM, s));
-    NA_CUDA(dg_launch_resolve(job, s));
+    DgLaunchCfg cfg;
+    cfg.cull_blocks = (unsigned)nsm * DG_CULL_BLOCKS_PER_SM;
+    cfg.setup_blocks = (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM;
+    cfg.queue_blocks = (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM;
+    cfg.shade_blocks = (unsigned)nsm * DG_SHADE_BLOCKS_PER_SM;
+    NA_CUDA(dg_launch_job(job, cfg, s, nullptr));
 
     if (status_out) {
         uint32_t err = 0;

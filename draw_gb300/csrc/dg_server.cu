@@ -192,21 +192,22 @@ void scheduler(dg_server* s) {
         if (free_slot && !s->pending.empty()) {
             // admit in arrival order while the batch size and the memory budget allow; the
             // budget covers the requests' buffers and the scratch growth of the batch
-            uint64_t V = 0, T = 0;
+            uint64_t V = 0, T = 0, P = 0;
             uint32_t L = 1;
             const uint64_t cur = free_slot->js.scratch_bytes;
             while (!s->pending.empty() && batch.size() < s->max_batch) {
                 Request* r = s->pending.front();
                 const Object& o = s->ctx->objects[r->scene.objects[0]];
-                const uint64_t V2 = V + o.nv, T2 = T + o.ntri_opaque;
+                const uint64_t V2 = V + o.nv, T2 = T + o.ntri_opaque, P2 = P + r->scene.width * r->scene.height;
                 const uint32_t L2 = std::max<uint32_t>(L, (uint32_t)r->scene.lights.size());
-                const uint64_t after = slot_scratch_after(free_slot->js, V2, T2, L2);
+                const uint64_t after = slot_scratch_after(free_slot->js, V2, T2, L2, P2);
                 const uint64_t grow_by = after > cur ? after - cur : 0;
                 if (s->used + r->bytes + (grow_by - reserved) > s->budget) break;
                 s->used += r->bytes + (grow_by - reserved);
                 reserved = grow_by;
                 V = V2;
                 T = T2;
+                P = P2;
                 L = L2;
                 s->peak_used = std::max(s->peak_used, s->used);
                 s->pending.pop_front();

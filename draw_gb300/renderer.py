@@ -143,6 +143,15 @@ def load_library() -> ctypes.CDLL:
     return lib
 
 
+# Kernels of one render job in launch order (dg_ctx_kernel_times).
+KERNELS = ["vertex", "cull", "setup_raster", "queue_raster", "resolve", "shade"]
+# dg_tuning fields in order.
+TUNING_KEYS = ["small_max_px", "setup_blocks_per_sm", "queue_blocks_per_sm", "cull_blocks_per_sm", "record_limit"]
+# dg_ctx_last_stats entries in order.
+STATS_KEYS = ["vertices", "triangles", "queued_triangles", "queued_units", "covered_pixels", "inplace_triangles",
+              "h2d_bytes", "launches", "survivors", "triangle_records", "clip_rows"]
+
+
 def _chk(st: int, what: str):
     if st != DG_OK:
         raise DrawError(st, what)
@@ -182,32 +191,31 @@ class Context:
         _chk(self.lib.dg_ctx_set_timing(self.h, 1 if on else 0), "set_timing")
 
     def kernel_times(self) -> dict:
-        ms = (ctypes.c_float * 4)()
-        _chk(self.lib.dg_ctx_kernel_times(self.h, ms, 4), "kernel_times")
-        return dict(zip(["vertex", "setup_raster", "queue_raster", "resolve"], list(ms)))
+        ms = (ctypes.c_float * len(KERNELS))()
+        _chk(self.lib.dg_ctx_kernel_times(self.h, ms, len(KERNELS)), "kernel_times")
+        return dict(zip(KERNELS, list(ms)))
 
-    def set_tuning(self, small_max_px: int = None, setup_blocks_per_sm: int = None, queue_blocks_per_sm: int = None):
-        """Raster knobs: in-warp raster threshold (bounding-box pixels) and grid sizes per SM.
-        None keeps the current value. Results do not depend on them; only speed does."""
+    def set_tuning(self, **knobs):
+        """Raster knobs (TUNING_KEYS): in-warp raster threshold (bounding-box pixels) and grid
+        sizes per SM; keys left out keep their value. Results do not depend on them, only speed."""
         t = self.get_tuning()
-        for k, v in (("small_max_px", small_max_px), ("setup_blocks_per_sm", setup_blocks_per_sm),
-                     ("queue_blocks_per_sm", queue_blocks_per_sm)):
+        for k, v in knobs.items():
+            if k not in t:
+                raise KeyError(k)
             if v is not None:
                 t[k] = int(v)
-        raw = (ctypes.c_uint32 * 3)(t["small_max_px"], t["setup_blocks_per_sm"], t["queue_blocks_per_sm"])
+        raw = (ctypes.c_uint32 * len(TUNING_KEYS))(*[t[k] for k in TUNING_KEYS])
         _chk(self.lib.dg_ctx_set_tuning(self.h, raw), "set_tuning")
 
     def get_tuning(self) -> dict:
-        raw = (ctypes.c_uint32 * 3)()
+        raw = (ctypes.c_uint32 * len(TUNING_KEYS))()
         _chk(self.lib.dg_ctx_get_tuning(self.h, raw), "get_tuning")
-        return dict(zip(["small_max_px", "setup_blocks_per_sm", "queue_blocks_per_sm"], list(raw)))
+        return dict(zip(TUNING_KEYS, list(raw)))
 
     def last_stats(self) -> dict:
-        v = (ctypes.c_uint64 * 8)()
-        _chk(self.lib.dg_ctx_last_stats(self.h, v, 8), "last_stats")
-        keys = ["vertices", "triangles", "queued_triangles", "queued_units", "covered_pixels", "queue_overflow",
-                "h2d_bytes", "launches"]
-        return dict(zip(keys, list(v)))
+        v = (ctypes.c_uint64 * len(STATS_KEYS))()
+        _chk(self.lib.dg_ctx_last_stats(self.h, v, len(STATS_KEYS)), "last_stats")
+        return dict(zip(STATS_KEYS, list(v)))
 
     def render_batch(self, scenes: list, canvases: list):
         """The batched form: all frames in one launch per pipeline stage."""

@@ -75,29 +75,35 @@ dg_status dg_ctx_synchronize(dg_ctx* ctx);
 /* Replaces the context's stream (cudaStream_t passed as void*; NULL = own stream). */
 dg_status dg_ctx_set_stream(dg_ctx* ctx, void* stream);
 void* dg_ctx_stream(dg_ctx* ctx);
-/* Per-kernel CUDA-event timing of the last render (ms); names: "vertex", "setup_raster",
- * "queue_raster", "resolve". Enabled with dg_ctx_set_timing(ctx, 1). */
+/* Per-kernel CUDA-event timing of the last render (ms), up to 6 values: "vertex", "cull",
+ * "setup_raster", "queue_raster", "resolve", "shade". Enabled with dg_ctx_set_timing(ctx, 1); the
+ * events between kernels also stop their launch overlap, so frames are slower meanwhile. */
 dg_status dg_ctx_set_timing(dg_ctx* ctx, int32_t enable);
 dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
 /* Launch-shape knobs of the raster passes (chosen by draw_gb300.autotune):
  * small_max_px: triangles whose clipped bounding box has at most this many
  * pixels are rasterized by the warp that sets them up, the others go to the
- * load-balanced queue pass (0 = all queued, max 4096); setup_blocks_per_sm and
- * queue_blocks_per_sm: grid sizes of those two passes in 256-thread blocks per
- * SM (1..64). Results do not depend on them. */
+ * load-balanced queue pass (0 = all queued, max 4096); setup_blocks_per_sm,
+ * queue_blocks_per_sm and cull_blocks_per_sm: grid sizes (caps) of those passes
+ * in 256-thread blocks per SM (1..64); record_limit: 0, or at most this many
+ * triangle records per render (triangles beyond it are shaded from the mesh
+ * again in the resolve pass). Results do not depend on them. */
 typedef struct {
     uint32_t small_max_px;
     uint32_t setup_blocks_per_sm;
     uint32_t queue_blocks_per_sm;
+    uint32_t cull_blocks_per_sm;
+    uint32_t record_limit;
 } dg_tuning;
 dg_status dg_ctx_set_tuning(dg_ctx* ctx, const dg_tuning* t);
 dg_status dg_ctx_get_tuning(dg_ctx* ctx, dg_tuning* t);
 
-/* Counters of the last render: [0] vertices, [1] input triangles, [2] triangles queued
- * for the load-balanced raster pass, [3] their 32-pixel work units, [4] covered pixels
- * (written by resolve), [5] queued triangles rasterized in place because the queue was
- * full, [6] host-to-device bytes of the job descriptor, [7] kernels launched.
- * Synchronizes. */
+/* Counters of the last render (up to 11): [0] vertices, [1] input triangles, [2] triangles
+ * queued for the load-balanced raster pass, [3] their 32-pixel work units, [4] covered
+ * pixels (written by resolve), [5] large triangles rasterized in place because the queue
+ * or the triangle records were full, [6] host-to-device bytes of the job descriptor,
+ * [7] kernels launched, [8] triangles that passed the cull pass, [9] triangle records
+ * handed out, [10] light/halfway rows handed out to clip vertices. Synchronizes. */
 dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
 
 /* -------------------------------------------------------------- texture map */

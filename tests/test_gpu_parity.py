@@ -97,18 +97,26 @@ def test_repeat_render_stable(gpu_ctx):
     assert np.array_equal(one[0], two[0]) and np.array_equal(one[1].view(np.uint32), two[1].view(np.uint32))
 
 
-@pytest.mark.parametrize("small,setup_bps,queue_bps", [(0, 16, 8), (4096, 16, 8), (32, 1, 1), (256, 64, 64)])
-def test_tuning_does_not_change_results(small, setup_bps, queue_bps, gpu_ctx, oracle_lib):
-    """The raster knobs only move work between the in-warp and queue rasterizers
-    and resize grids; coverage, depth and colour stay bit-identical."""
+@pytest.mark.parametrize("knobs", [
+    dict(small_max_px=0), dict(small_max_px=4096),
+    dict(setup_blocks_per_sm=1, queue_blocks_per_sm=1, cull_blocks_per_sm=1),
+    dict(small_max_px=256, setup_blocks_per_sm=64, queue_blocks_per_sm=64, cull_blocks_per_sm=64),
+    dict(record_limit=1), dict(record_limit=200, small_max_px=0)])
+def test_tuning_does_not_change_results(knobs, gpu_ctx, oracle_lib):
+    """The raster knobs only move work between the in-warp and queue rasterizers,
+    resize grids, or (record_limit) send triangles without a record through the
+    resolve pass's own setup; coverage, depth and colour stay bit-identical."""
     before = gpu_ctx.get_tuning()
     try:
-        gpu_ctx.set_tuning(small_max_px=small, setup_blocks_per_sm=setup_bps, queue_blocks_per_sm=queue_bps)
+        gpu_ctx.set_tuning(**knobs)
         for name in ("torus_strict", "sphere_field_small", "clip"):
             desc = cases.PARITY_CASES[name]()
             ref = oracle_render(desc)
             got = gpu_render(desc, gpu_ctx)
             p = compare(ref, got, desc.clear_depth)
-            assert p.ok, f"{name} {small}/{setup_bps}/{queue_bps}: {describe(p)}; {first_mismatch(ref, got)}"
+            assert p.ok, f"{name} {knobs}: {describe(p)}; {first_mismatch(ref, got)}"
+            st = gpu_ctx.last_stats()
+            if knobs.get("record_limit") == 1:
+                assert st["triangle_records"] > 1  # some triangles went without a record
     finally:
         gpu_ctx.set_tuning(**before)

@@ -143,13 +143,13 @@ def test_host_only_context_refuses_device_work(lib):
 
 def test_tuning_round_trip_and_validation(lib):
     h = host_ctx(lib)
-    t = (ctypes.c_uint32 * 3)()
+    t = (ctypes.c_uint32 * 5)()
     assert lib.dg_ctx_get_tuning(h, t) == 0
-    assert list(t) == [32, 16, 8]
-    assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 3)(0, 1, 64)) == 0
-    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64]
-    for bad in ((4097, 16, 8), (32, 0, 8), (32, 16, 65)):
-        assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 3)(*bad)) == 1
-    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64]
+    assert list(t) == [32, 4, 8, 32, 0]
+    assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 5)(0, 1, 64, 2, 7)) == 0
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64, 2, 7]
+    for bad in ((4097, 16, 8, 32, 0), (32, 0, 8, 32, 0), (32, 16, 65, 32, 0), (32, 16, 8, 0, 0)):
+        assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 5)(*bad)) == 1
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64, 2, 7]
     assert lib.dg_ctx_set_tuning(h, None) == 1
     lib.dg_ctx_destroy(h)
