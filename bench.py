@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-stress", action="store_true", help="skip the stress leg")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--batch-frames", type=int, default=256)
@@ -79,8 +80,8 @@ def algorithmic_bytes(desc, stats: dict) -> dict:
     index triples (12 B per triangle); setup_raster, for each surviving
     triangle, its uv and normal index triples and the six attribute vectors
     (24 + 3*12 + 3*8 = 84 B); queue_raster moves only intermediate data;
-    resolve writes colour + depth of the empty pixels (8 B each); shade reads
-    the texture maps once and writes colour + depth of the covered pixels."""
+    resolve writes colour + depth of every pixel (8 B each) and reads the
+    texture maps once."""
     V = sum(o.vertices.shape[0] for o in desc.objects)
     N = sum(o.normals.shape[0] for o in desc.objects)
     U = sum(o.uvs.shape[0] for o in desc.objects)
@@ -93,8 +94,7 @@ def algorithmic_bytes(desc, stats: dict) -> dict:
         "cull": T * 12,
         "setup_raster": int(stats["survivors"]) * 84,
         "queue_raster": 0,
-        "resolve": (W * H - C) * 8,
-        "shade": C * 8 + tex,
+        "resolve": W * H * 8 + tex,
     }
     per["frame"] = V * 12 + N * 12 + U * 8 + T * 36 + tex + W * H * 8
     return per
@@ -413,6 +413,9 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_serve:
         line["served"] = serving_leg(local, seconds=args.serve_seconds, rate=args.serve_rate)
 
+    if rank == 0 and world == 1 and not args.no_stress:
+        line["stress"] = stress_leg(ctx, stream, flush, peak, cpu=not args.no_cpu)
+
     if rank == 0 and world == 1 and not args.no_cpu:
         bgra, depth = canvas.read()
         threads = os.cpu_count() or 1
@@ -466,12 +469,108 @@ def batched_leg(ctx, stream, n_frames: int) -> dict:
         torch.cuda.synchronize()
     plain_ms = e[0].elapsed_time(e[1]) / reps
     batch_ms = e[2].elapsed_time(e[3]) / reps
+
+    def graph_ms():
+        g = ctx.batch(sc, cv)
+        try:
+            for _ in range(2):
+                g.render()
+            torch.cuda.synchronize()
+            e[0].record(stream)
+            for _ in range(reps):
+                g.render()
+            e[1].record(stream)
+            torch.cuda.synchronize()
+            return e[0].elapsed_time(e[1]) / reps, g.info()
+        finally:
+            g.close()
+
+    with torch.cuda.stream(stream):
+        graph_default_ms, ginfo = graph_ms()
+        before = ctx.get_tuning()
+        t0 = time.perf_counter()
+        tuned, _ = ctx.autotune(sc, cv, reps=2)
+        tune_s = time.perf_counter() - t0
+        graph_tuned_ms, _ = graph_ms()
+        ctx.set_tuning(**before)
+    graph_ms_best = min(graph_default_ms, graph_tuned_ms)
     tris = sum(d.n_tris for d in frames)
     out = {"frames": n_frames, "triangles": tris, "pixels": sum(d.width * d.height for d in frames),
            "plain_frames_per_s": n_frames / (plain_ms * 1e-3), "batched_frames_per_s": n_frames / (batch_ms * 1e-3),
            "speedup": plain_ms / batch_ms, "batched_mtris_per_s": tris / (batch_ms * 1e-3) / 1e6,
+           "graph_frames_per_s": n_frames / (graph_default_ms * 1e-3),
+           "graph_tuned_frames_per_s": n_frames / (graph_tuned_ms * 1e-3),
+           "graph_speedup": plain_ms / graph_ms_best, "graph_kernels_per_replay": int(ginfo["kernels_per_replay"]),
+           "autotuned": tuned, "autotune_s": tune_s,
            "workload": "256 frames, side log-uniform 128..512, 1k..200k triangles (torus/sphere), "
-                       "textures 256^2..1024^2 from a pool of 32; L2 not flushed (working set > L2)"}
+                       "textures 256^2..1024^2 from a pool of 32; L2 not flushed (working set > L2); "
+                       "batched = one launch per stage for all frames; graph = the same job replayed from a "
+                       "CUDA graph (dg_batch_render), with the default and the autotuned launch shapes"}
+    return out
+
+
+def stress_leg(ctx, stream, flush, peak: float, steps: int = 20, cpu: bool = True) -> dict:
+    """Stress config: one 3840x2160 frame of 10M micro-sphere triangles, 4096^2
+    texture, 4 lights; device time per frame (L2 flushed before each), with the
+    default and the autotuned launch shapes, parity against the CPU oracle and
+    the oracle's single-thread frame time."""
+    import numpy as np
+    import torch
+
+    from draw_gb300 import renderer, scenes
+
+    t0 = time.perf_counter()
+    desc = scenes.micro_sphere_field()
+    b = renderer.build_scene(desc, ctx)
+    gen_s = time.perf_counter() - t0
+
+    def timed():
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                flush.zero_()
+                b.scene.render(b.canvas)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            tot = 0.0
+            for _ in range(steps):
+                flush.zero_()
+                e0.record(stream)
+                b.scene.render(b.canvas)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                tot += e0.elapsed_time(e1)
+        return tot / steps
+
+    before = ctx.get_tuning()
+    ms_default = timed()
+    stats = ctx.last_stats()
+    with torch.cuda.stream(stream):
+        tuned, _ = ctx.autotune([b.scene], [b.canvas], reps=2)
+    ms_tuned = timed()
+    ctx.set_tuning(**before)
+    ms = min(ms_default, ms_tuned)
+    ab = algorithmic_bytes(desc, stats)
+    out = {"workload": "3840x2160, 10,000,000 micro-sphere triangles (250,000 spheres x 40), 4096^2 RGBA8 texture, "
+                       "4 point lights; L2 flushed before every frame",
+           "near_crossing": desc.near_crossing, "depth_complexity_est": desc.depth_complexity_est,
+           "mean_tri_px_est": desc.mean_tri_px_est, "build_s": gen_s,
+           "ms_per_frame_default": ms_default, "ms_per_frame_tuned": ms_tuned, "autotuned": tuned,
+           "frames_per_s": 1000.0 / ms, "mtris_per_s": desc.n_tris / (ms * 1e-3) / 1e6,
+           "mshaded_frags_per_s": stats["covered_pixels"] / (ms * 1e-3) / 1e6,
+           "frame_roofline": {"achieved": ab["frame"] / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                              "frac": ab["frame"] / (ms * 1e-3) / 1e9 / peak, "algorithmic_bytes": ab["frame"]},
+           "frame_stats": {k: int(v) for k, v in stats.items()}}
+    if cpu:
+        farm = OracleFarm(desc, 1)
+        t1, ref = farm.single()
+        farm.close()
+        with torch.cuda.stream(stream):
+            b.scene.render(b.canvas)
+        bgra, depth = b.canvas.read()
+        diff = np.abs(ref.bgra.astype(np.int16) - bgra.astype(np.int16))
+        out["cpu_single_thread_ms"] = t1 * 1000.0
+        out["parity"] = {"depth_bits_equal": bool(np.array_equal(ref.depth.view(np.uint32), depth.view(np.uint32))),
+                         "colour_max_lsb": int(diff.max()), "colour_frac_diff": float((diff.max(-1) > 0).mean())}
     return out
 
 

@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
-SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu"]
+SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu"]
 HEADERS = ["dg_internal.cuh", "dg_host.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -284,11 +284,14 @@ Object* get_object(dg_ctx* c, int32_t id) {
     return &c->objects[id];
 }
 
-// dg_scene_render / dg_render_batch: resolves ids, then launches on the context slot.
-dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n) {
-    if (n == 0) return DG_OK;
-    std::vector<Scene*> sc(n);
-    std::vector<FrameTarget> tg(n);
+}  // namespace
+
+namespace dgh {
+
+dg_status resolve_frames(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n,
+                         std::vector<Scene*>& sc, std::vector<FrameTarget>& tg) {
+    sc.resize(n);
+    tg.resize(n);
     for (uint32_t i = 0; i < n; i++) {
         Scene* s = get_scene(c, scenes[i]);
         Canvas* cv = get_canvas(c, canvases[i]);
@@ -297,10 +300,20 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
         sc[i] = s;
         tg[i] = FrameTarget{cv->d_colour, cv->d_depth, cv->d_vis, cv->w, cv->h, cv->depth_max, cv->off_x, cv->off_y};
     }
+    return DG_OK;
+}
+
+// dg_scene_render / dg_render_batch: resolves ids, then launches on the context slot.
+dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n) {
+    if (n == 0) return DG_OK;
+    std::vector<Scene*> sc;
+    std::vector<FrameTarget> tg;
+    dg_status e = resolve_frames(c, scenes, canvases, n, sc, tg);
+    if (e) return e;
     return launch_frames(c, c->main, sc.data(), tg.data(), n);
 }
 
-}  // namespace
+}  // namespace dgh
 
 namespace dgh {
 
@@ -328,11 +341,12 @@ void slot_free(JobSlot& s) {
     dfree(s.d_vshade);
     dfree(s.d_vmark);
     dfree(s.d_queue);
+    dfree(s.d_small);
+    dfree(s.d_fb);
     dfree(s.d_items);
     dfree(s.d_surv);
     dfree(s.d_rec_of);
     dfree(s.d_trec);
-    dfree(s.d_shade);
     dfree(s.d_counters);
     dfree(s.d_err);
     for (int i = 0; i < JobSlot::kStage; i++) {
@@ -407,21 +421,24 @@ uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L
     const size_t vshade = cap_after(s.vshade_cap, s.d_vshade, (V + dg_vrow_extra(T)) * L * 2);
     const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>((V + 31) / 32, 1));
     const size_t q = cap_after(s.queue_cap, s.d_queue, queue_records(T));
+    const size_t sm = cap_after(s.small_cap, s.d_small, queue_records(T));
+    const size_t fb = cap_after(s.fb_cap, s.d_fb, P / ((uint64_t)DG_TILE_W * 8u) + 65536u);  // tiles, any tile_rows
     const size_t qb = cap_after(s.items_cap, s.d_items, dg_items_cap(q));
     const size_t sv = cap_after(s.surv_cap, s.d_surv, std::max<uint64_t>(T, 1));
     const size_t ro = cap_after(s.rec_of_cap, s.d_rec_of, std::max<uint64_t>(T, 1));
     const size_t tr = cap_after(s.trec_cap, s.d_trec, trec_records(T));
-    const size_t sh = cap_after(s.shade_cap, s.d_shade, std::max<uint64_t>(P, 1));
-    return vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + q * sizeof(DgQueueRec) +
-           qb * sizeof(uint2) + (sv + ro) * sizeof(uint32_t) + tr * sizeof(DgTriRec) + sh * sizeof(uint2);
+    return vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + (q + sm) * sizeof(DgQueueRec) +
+           qb * sizeof(uint2) + (sv + ro + fb) * sizeof(uint32_t) + tr * sizeof(DgTriRec);
 }
 
-dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n) {
-    if (n == 0) return DG_OK;
+dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n,
+                    JobBuild& B) {
     dg_status e = set_device(c);
     if (e) return e;
-    std::vector<DgFrameDev> frames(n);
-    std::vector<DgSegDev> segs;
+    std::vector<DgFrameDev>& frames = B.frames;
+    std::vector<DgSegDev>& segs = B.segs;
+    frames.assign(n, DgFrameDev{});
+    segs.clear();
     uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0, total_px = 0;
     uint32_t stride = 1;
     for (uint32_t i = 0; i < n; i++) {
@@ -457,7 +474,7 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
         f.seg_begin = (uint32_t)segs.size();
         f.tile_begin = (uint32_t)total_tiles;
         f.tiles_x = (uint32_t)((tg.w + DG_TILE_W - 1) / DG_TILE_W);
-        total_tiles += (uint64_t)f.tiles_x * ((tg.h + DG_TILE_H - 1) / DG_TILE_H);
+        total_tiles += (uint64_t)f.tiles_x * ((tg.h + S.tile_rows - 1) / S.tile_rows);
         f.pix_begin = (uint32_t)total_px;
         total_px += tg.w * tg.h;
         if (total_px >= 0x80000000ull) return DG_E_LIMIT;  // job-wide pixel indices use 31 bits
@@ -507,8 +524,6 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     if (e) return e;
     e = grow(S, &S.d_trec, &S.trec_cap, trec_records(total_tri));
     if (e) return e;
-    e = grow(S, &S.d_shade, &S.shade_cap, std::max<uint64_t>(total_px, 1));
-    if (e) return e;
     const size_t want_mark = std::max<uint64_t>((total_vtx + 31) / 32, 1);
     if (S.vmark_cap < want_mark) {
         e = grow(S, &S.d_vmark, &S.vmark_cap, want_mark);
@@ -522,33 +537,17 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
         e = grow(S, &S.d_items, &S.items_cap, dg_items_cap(S.queue_cap));
         if (e) return e;
     }
-
-    // job descriptor upload through a pinned staging slot
-    const size_t fbytes = frames.size() * sizeof(DgFrameDev), sbytes = segs.size() * sizeof(DgSegDev);
-    const size_t need = fbytes + sbytes;
-    const int k = S.stage;
-    S.stage = (S.stage + 1) % JobSlot::kStage;
-    DG_CUDA(cudaEventSynchronize(S.stage_ev[k]));
-    if (S.stage_cap[k] < need) {
-        if (S.h_stage[k]) cudaFreeHost(S.h_stage[k]);
-        dfree(S.d_stage[k]);
-        S.h_stage[k] = nullptr;
-        S.stage_cap[k] = 0;
-        size_t cap = std::max<size_t>(need * 2, 64 * 1024);
-        DG_CUDA(cudaMallocHost(&S.h_stage[k], cap));
-        e = dalloc((uint8_t**)&S.d_stage[k], cap);
+    e = grow(S, &S.d_fb, &S.fb_cap, std::max<uint64_t>(total_tiles, 1));
+    if (e) return e;
+    if (S.small_cap < want_queue) {
+        e = grow(S, &S.d_small, &S.small_cap, want_queue);
         if (e) return e;
-        S.stage_cap[k] = cap;
     }
-    std::memcpy(S.h_stage[k], frames.data(), fbytes);
-    std::memcpy((uint8_t*)S.h_stage[k] + fbytes, segs.data(), sbytes);
-    DG_CUDA(cudaMemcpyAsync(S.d_stage[k], S.h_stage[k], need, cudaMemcpyHostToDevice, S.stream));
-    DG_CUDA(cudaEventRecord(S.stage_ev[k], S.stream));
 
-    DgJobDev job;
+    B.fbytes = frames.size() * sizeof(DgFrameDev);
+    B.sbytes = segs.size() * sizeof(DgSegDev);
+    DgJobDev& job = B.job;
     std::memset(&job, 0, sizeof(job));
-    job.frames = (const DgFrameDev*)S.d_stage[k];
-    job.segs = (const DgSegDev*)((uint8_t*)S.d_stage[k] + fbytes);
     job.nframes = n;
     job.nsegs = (uint32_t)segs.size();
     job.total_vtx = (uint32_t)total_vtx;
@@ -565,28 +564,69 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     job.trec_cap = (uint32_t)std::min<size_t>(S.trec_cap, 0xFFFFFFF0ull);
     if (S.record_limit) job.trec_cap = std::min(job.trec_cap, S.record_limit);
     job.queue = S.d_queue;
+    job.small = S.d_small;
+    job.small_cap = (uint32_t)std::min<size_t>(S.small_cap, 0xFFFFFFF0ull);
     job.items = S.d_items;
     job.items_cap = (uint32_t)std::min<size_t>(S.items_cap, 0xFFFFFFF0ull);
     job.queue_cap = (uint32_t)std::min<size_t>(S.queue_cap, (1u << 24) - 1);
     job.small_max_px = S.small_max_px;
+    job.item_units = S.item_units;
     job.cnt = S.d_counters;
     job.total_px = (uint32_t)total_px;
-    job.shade_list = S.d_shade;
+    job.tile_rows = S.tile_rows;
+    job.fb_tiles = S.d_fb;
     job.tex = c->d_tex;
     job.ntex = (uint32_t)c->tex.size();
     job.err = S.d_err;
-    S.last_vtx = total_vtx;
-    S.last_tri = total_tri;
-    S.last_h2d = need;
-    S.last_launches = (total_vtx ? 1 : 0) + (total_tri ? 3 : 0) + (total_tiles ? 1 : 0) + (total_px ? 1 : 0);
+    B.launches = (total_vtx ? 1 : 0) + (total_tri ? 3 : 0) + (total_tiles ? 2 : 0);
+    B.cfg.cull_blocks = (unsigned)c->nsm * S.cull_blocks_per_sm;
+    B.cfg.setup_blocks = (unsigned)c->nsm * S.setup_blocks_per_sm;
+    B.cfg.queue_blocks = (unsigned)c->nsm * S.queue_blocks_per_sm;
+    B.cfg.fallback_blocks = (unsigned)c->nsm;
+    B.total_vtx = total_vtx;
+    B.total_tri = total_tri;
+    return DG_OK;
+}
 
-    DG_CUDA(cudaMemsetAsync(S.d_counters, 0, DG_NCOUNTERS * sizeof(unsigned long long), S.stream));
-    DgLaunchCfg cfg;
-    cfg.cull_blocks = (unsigned)c->nsm * S.cull_blocks_per_sm;
-    cfg.setup_blocks = (unsigned)c->nsm * S.setup_blocks_per_sm;
-    cfg.queue_blocks = (unsigned)c->nsm * S.queue_blocks_per_sm;
-    cfg.shade_blocks = (unsigned)c->nsm * DG_SHADE_BLOCKS_PER_SM;
-    DG_CUDA(dg_launch_job(job, cfg, S.stream, S.timing ? S.ev : nullptr));
+dg_status enqueue_job(JobBuild& B, JobSlot& S, void* d_stage, cudaStream_t stream, bool timing) {
+    B.job.frames = (const DgFrameDev*)d_stage;
+    B.job.segs = (const DgSegDev*)((uint8_t*)d_stage + B.fbytes);
+    DG_CUDA(cudaMemsetAsync(S.d_counters, 0, DG_NCOUNTERS * sizeof(unsigned long long), stream));
+    DG_CUDA(dg_launch_job(B.job, B.cfg, stream, timing ? S.ev : nullptr));
+    return DG_OK;
+}
+
+dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n) {
+    if (n == 0) return DG_OK;
+    JobBuild B;
+    dg_status e = build_job(c, S, scenes, targets, n, B);
+    if (e) return e;
+    // job descriptor upload through a pinned staging slot
+    const size_t need = B.fbytes + B.sbytes;
+    const int k = S.stage;
+    S.stage = (S.stage + 1) % JobSlot::kStage;
+    DG_CUDA(cudaEventSynchronize(S.stage_ev[k]));
+    if (S.stage_cap[k] < need) {
+        if (S.h_stage[k]) cudaFreeHost(S.h_stage[k]);
+        dfree(S.d_stage[k]);
+        S.h_stage[k] = nullptr;
+        S.stage_cap[k] = 0;
+        size_t cap = std::max<size_t>(need * 2, 64 * 1024);
+        DG_CUDA(cudaMallocHost(&S.h_stage[k], cap));
+        e = dalloc((uint8_t**)&S.d_stage[k], cap);
+        if (e) return e;
+        S.stage_cap[k] = cap;
+    }
+    std::memcpy(S.h_stage[k], B.frames.data(), B.fbytes);
+    std::memcpy((uint8_t*)S.h_stage[k] + B.fbytes, B.segs.data(), B.sbytes);
+    DG_CUDA(cudaMemcpyAsync(S.d_stage[k], S.h_stage[k], need, cudaMemcpyHostToDevice, S.stream));
+    DG_CUDA(cudaEventRecord(S.stage_ev[k], S.stream));
+    S.last_vtx = B.total_vtx;
+    S.last_tri = B.total_tri;
+    S.last_h2d = need;
+    S.last_launches = B.launches;
+    e = enqueue_job(B, S, S.d_stage[k], S.stream, S.timing);
+    if (e) return e;
     if (S.timing) S.ev_valid = true;
     return DG_OK;
 }
@@ -720,13 +760,16 @@ dg_status dg_ctx_set_tuning(dg_ctx* c, const dg_tuning* t) {
     if (!c || !t) return DG_E_INVALID;
     auto bad = [](uint32_t b) { return b < 1 || b > 64; };
     if (t->small_max_px > 4096 || bad(t->setup_blocks_per_sm) || bad(t->queue_blocks_per_sm) ||
-        bad(t->cull_blocks_per_sm))
+        bad(t->cull_blocks_per_sm) || (t->tile_rows != 8 && t->tile_rows != 16 && t->tile_rows != 32) ||
+        t->item_units < 1 || t->item_units > 256)
         return DG_E_INVALID;
     c->main.small_max_px = t->small_max_px;
     c->main.setup_blocks_per_sm = t->setup_blocks_per_sm;
     c->main.queue_blocks_per_sm = t->queue_blocks_per_sm;
     c->main.cull_blocks_per_sm = t->cull_blocks_per_sm;
     c->main.record_limit = t->record_limit;
+    c->main.tile_rows = t->tile_rows;
+    c->main.item_units = t->item_units;
     return DG_OK;
 }
 
@@ -737,6 +780,8 @@ dg_status dg_ctx_get_tuning(dg_ctx* c, dg_tuning* t) {
     t->queue_blocks_per_sm = c->main.queue_blocks_per_sm;
     t->cull_blocks_per_sm = c->main.cull_blocks_per_sm;
     t->record_limit = c->main.record_limit;
+    t->tile_rows = c->main.tile_rows;
+    t->item_units = c->main.item_units;
     return DG_OK;
 }
 
@@ -747,7 +792,7 @@ dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
     DG_CUDA(cudaStreamSynchronize(S.stream));
     unsigned long long h[DG_NCOUNTERS];
     DG_CUDA(cudaMemcpy(h, S.d_counters, sizeof(h), cudaMemcpyDeviceToHost));
-    const uint64_t v[11] = {S.last_vtx,
+    const uint64_t v[12] = {S.last_vtx,
                             S.last_tri,
                             h[DG_CNT_QUEUE] >> DG_PACK_SHIFT,
                             h[DG_CNT_UNITS],
@@ -757,8 +802,9 @@ dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
                             S.last_launches,
                             h[DG_CNT_SURV],
                             h[DG_CNT_TREC],
-                            h[DG_CNT_VROW]};
-    for (int i = 0; i < n && i < 11; i++) out[i] = v[i];
+                            h[DG_CNT_VROW],
+                            h[DG_CNT_SMALL]};
+    for (int i = 0; i < n && i < 12; i++) out[i] = v[i];
     return DG_OK;
 }
 

@@ -111,6 +111,10 @@ struct JobSlot {
     uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
     size_t vmark_cap = 0;
     DgQueueRec* d_queue = nullptr;
+    DgQueueRec* d_small = nullptr;  // small-triangle list
+    size_t small_cap = 0;
+    uint32_t* d_fb = nullptr;  // resolve fallback tile list
+    size_t fb_cap = 0;
     uint2* d_items = nullptr;  // raster work items
     size_t queue_cap = 0;
     size_t items_cap = 0;
@@ -120,12 +124,12 @@ struct JobSlot {
     size_t rec_of_cap = 0;
     DgTriRec* d_trec = nullptr;
     size_t trec_cap = 0;
-    uint2* d_shade = nullptr;  // shade list (one entry per pixel of the job)
-    size_t shade_cap = 0;
     uint32_t small_max_px = DG_SMALL_MAX_PX;  // dg_tuning knobs
     uint32_t setup_blocks_per_sm = DG_SETUP_BLOCKS_PER_SM;
     uint32_t queue_blocks_per_sm = DG_QUEUE_BLOCKS_PER_SM;
     uint32_t cull_blocks_per_sm = DG_CULL_BLOCKS_PER_SM;
+    uint32_t tile_rows = DG_TILE_H;
+    uint32_t item_units = DG_ITEM_UNITS;
     uint32_t record_limit = 0;
     unsigned long long* d_counters = nullptr;  // DG_NCOUNTERS job counters (DG_CNT_*)
     uint32_t* d_err = nullptr;
@@ -172,5 +176,30 @@ dg_status sync_tex_table(dg_ctx* c, cudaStream_t s);
 uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L, uint64_t P);
 // Builds and launches one render job over n frames on slot s (asynchronous).
 dg_status launch_frames(dg_ctx* c, JobSlot& s, Scene* const* scenes, const FrameTarget* targets, uint32_t n);
+
+// Host part of one render job: the per-frame and per-segment descriptors (the
+// bytes uploaded before the kernels run), the job descriptor the kernels take
+// by value (its frames/segs pointers are set by enqueue_job) and the grid sizes.
+struct JobBuild {
+    std::vector<DgFrameDev> frames;
+    std::vector<DgSegDev> segs;
+    size_t fbytes = 0, sbytes = 0;
+    DgJobDev job{};
+    DgLaunchCfg cfg{};
+    uint64_t total_vtx = 0, total_tri = 0, launches = 0;
+};
+// Host frame setup of every frame (camera basis, matrix, view planes) and the
+// scratch sizing of slot s (grows its buffers; synchronizes s only when one grows).
+dg_status build_job(dg_ctx* c, JobSlot& s, Scene* const* scenes, const FrameTarget* targets, uint32_t n,
+                    JobBuild& b);
+// Resolves scene and canvas ids into frames (DG_E_INVALID for a bad id,
+// DG_E_DEPTH_UNINIT for a canvas without init_depth).
+dg_status resolve_frames(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n,
+                         std::vector<Scene*>& sc, std::vector<FrameTarget>& tg);
+// dg_scene_render / dg_render_batch on the context's own slot and stream.
+dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n);
+// Enqueues the counter reset and the kernels of a built job whose descriptors
+// are (or will be, in stream order) at d_stage on the device.
+dg_status enqueue_job(JobBuild& b, JobSlot& s, void* d_stage, cudaStream_t stream, bool timing);
 
 }  // namespace dgh

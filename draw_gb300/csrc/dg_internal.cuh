@@ -23,15 +23,17 @@
 #define DG_MAXL DG_MAX_LIGHTS
 #define DG_VIS_EMPTY 0xFFFFFFFFFFFFFFFFull
 
-// Triangles whose clipped bounding box has at most this many pixels are
-// rasterized by the warp that set them up (default of DgJobDev.small_max_px);
-// larger ones go to the raster queue: their row-major bounding-box pixels are
-// cut into units of DG_UNIT_PX (one per lane of a warp) and the units into work
-// items of at most DG_ITEM_UNITS, which the queue pass spreads over all warps.
-#define DG_SMALL_MAX_PX 32u
+// Triangles whose clipped bounding box has at most this many pixels go to the
+// small-triangle list, whose entries the queue pass rasterizes one per lane
+// (default of DgJobDev.small_max_px); larger ones go to the raster queue: their
+// row-major bounding-box pixels are cut into units of DG_UNIT_PX (one per lane
+// of a warp) and the units into work items of at most DgJobDev.item_units
+// (default DG_ITEM_UNITS), which the queue pass spreads over all warps.
+#define DG_SMALL_MAX_PX 16u
 #define DG_UNIT_PX 32u
 #define DG_ITEM_UNITS 8u
-// Resolve tile: 32 x 32 pixels, one CTA of 256 threads (four rows each).
+// Resolve tile: 32 x tile_rows pixels (tile_rows 8, 16 or 32; default
+// DG_TILE_H), one CTA of 256 threads.
 #define DG_TILE_W 32u
 #define DG_TILE_H 32u
 #define DG_PACK_SHIFT 40
@@ -129,7 +131,10 @@ struct alignas(16) DgTriRec {
 };
 static_assert(sizeof(DgTriRec) == 192, "triangle record size");
 
-// A triangle queued for the load-balanced raster pass (32 bytes).
+// A triangle queued for the load-balanced raster pass (32 bytes). Its clipped
+// bounding box's pixels, numbered row-major, are cut into units of DG_UNIT_PX
+// consecutive pixels, one per lane. Entries of the small-triangle list use the
+// same layout with npx holding the box height and nunits unused.
 struct alignas(16) DgQueueRec {
     uint32_t rec;     // its DgTriRec
     uint32_t seq;     // frame-local key low word
@@ -143,13 +148,16 @@ struct alignas(16) DgQueueRec {
 #define DG_NONE 0xFFFFFFFFu
 // Job counters (unsigned long long each).
 #define DG_CNT_QUEUE 0    // (queued records << DG_PACK_SHIFT) | work items
-#define DG_CNT_COVERED 1  // covered pixels (entries of the shade list)
+#define DG_CNT_COVERED 1  // covered pixels (shaded by the resolve pass)
 #define DG_CNT_INPLACE 2  // large triangles rasterized by their own lane (queue or record overflow)
 #define DG_CNT_SURV 3     // triangles that passed the cull pass
-#define DG_CNT_TREC 4     // triangle records handed out
+#define DG_CNT_TREC 4     // triangle records requested (statistics)
 #define DG_CNT_VROW 5     // light/halfway rows handed out to clip vertices
 #define DG_CNT_UNITS 6    // work units of the queued triangles
-#define DG_NCOUNTERS 8
+#define DG_CNT_SMALL 7    // entries of the small-triangle list
+#define DG_CNT_TRECX 8    // records handed out after the first total_tri (multi-output clips)
+#define DG_CNT_FBTILES 9  // entries of the fallback tile list
+#define DG_NCOUNTERS 10
 
 struct DgJobDev {
     const DgFrameDev* frames;
@@ -169,9 +177,13 @@ struct DgJobDev {
     DgQueueRec* queue;
     uint2* items;           // work items: (queue record, first unit)
     uint32_t items_cap;
-    uint32_t small_max_px;  // in-warp raster threshold (bounding-box pixels)
+    DgQueueRec* small;      // small-triangle list (nunits unused), rasterized one triangle per lane
+    uint32_t small_cap;
+    uint32_t small_max_px;  // small-triangle threshold (bounding-box pixels)
+    uint32_t item_units;    // work units per raster work item (>= 1)
     uint32_t total_px;      // pixels of all frames
-    uint2* shade_list;      // [total_px] (job-wide pixel index, key low word) of the covered pixels
+    uint32_t tile_rows;     // resolve tile height (8, 16 or 32)
+    uint32_t* fb_tiles;     // [total_tiles] tiles with pixels whose triangle has no record
     unsigned long long* cnt;  // DG_NCOUNTERS job counters, zero at the start of the job
     const DgTexDev* tex;
     uint32_t ntex;          // entries of tex
@@ -183,18 +195,17 @@ struct DgLaunchCfg {
     unsigned cull_blocks;   // grid caps / sizes in 256-thread blocks
     unsigned setup_blocks;
     unsigned queue_blocks;
-    unsigned shade_blocks;
+    unsigned fallback_blocks;
 };
 #define DG_SETUP_BLOCKS_PER_SM 4u
 #define DG_QUEUE_BLOCKS_PER_SM 8u
 #define DG_CULL_BLOCKS_PER_SM 32u
-#define DG_SHADE_BLOCKS_PER_SM 8u
-#define DG_NKERNELS 6  // vertex, cull, setup_raster, queue_raster, resolve, shade
+#define DG_NKERNELS 5  // vertex, cull, setup_raster, queue_raster, resolve
 // Launches the whole pipeline of one job on stream s. ev, if not null, holds
 // DG_NKERNELS + 1 events recorded around the kernels (per-kernel timing).
 cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev);
 // Scratch rows and records sized for a job of T triangles (shared sizing rule).
-constexpr uint64_t dg_trec_cap(uint64_t T) { return T + 4096u; }
+constexpr uint64_t dg_trec_cap(uint64_t T) { return T + T / 8u + 4096u; }
 constexpr uint64_t dg_items_cap(uint64_t queue_cap) { return 2u * queue_cap + 65536u; }
 constexpr uint64_t dg_vrow_extra(uint64_t T) { uint64_t x = 65536u + T / 8u; return x < 6u * T + 6u ? x : 6u * T + 6u; }
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,

@@ -14,10 +14,10 @@
 //   k_queue_raster  light/halfway vectors of the marked vertices, then the
 //                   queued triangles' bounding-box pixels in 32-pixel units
 //                   spread evenly over all warps
-//   k_resolve       per pixel: empty pixels get the clear colour/depth, covered
-//                   ones are compacted into the shade list
-//   k_shade         per covered pixel: the winning fragment is shaded once
-//                   (canvas.rs:682-745, 906-930) and colour/depth are written
+//   k_resolve       per 32 x tile_rows tile: empty pixels get the clear colour
+//                   and depth, covered ones are compacted into the tile's
+//                   shade list and their winning fragment is shaded once
+//                   (canvas.rs:682-745, 906-930)
 //
 // Exactness. The reference writes a fragment when its depth is strictly below
 // the stored depth (canvas.rs:923) and processes fragments in submission
@@ -163,17 +163,22 @@ __device__ __forceinline__ bool prereject(float n, float d) {
     return finite && ((n < 0.0f && !neg_d) || (n > 0.0f && neg_d));
 }
 
-// canvas.rs:673-681: the barycentric coverage test with the (-1,-1) tie rule.
-__device__ __forceinline__ bool covered(const EdgeSet& e, float x, float y, float& al, float& be, float& ga) {
-    float n0 = edge_eval(e, 0, x, y);
-    float n1 = edge_eval(e, 1, x, y);
-    float n2 = edge_eval(e, 2, x, y);
-    if (prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2])) return false;
+// canvas.rs:673-681: the barycentric coverage test with the (-1,-1) tie rule,
+// for a pixel whose edge values n0..n2 passed prereject.
+__device__ __forceinline__ bool covered_divide(const EdgeSet& e, float n0, float n1, float n2, float& al, float& be,
+                                               float& ga) {
     al = fD(n0, e.den[0]);
     be = fD(n1, e.den[1]);
     ga = fD(n2, e.den[2]);
     if (!(al >= 0.0f && be >= 0.0f && ga >= 0.0f)) return false;
     return (al > 0.0f || (e.tie & 1u)) && (be > 0.0f || (e.tie & 2u)) && (ga > 0.0f || (e.tie & 4u));
+}
+__device__ __forceinline__ bool covered(const EdgeSet& e, float x, float y, float& al, float& be, float& ga) {
+    const float n0 = edge_eval(e, 0, x, y);
+    const float n1 = edge_eval(e, 1, x, y);
+    const float n2 = edge_eval(e, 2, x, y);
+    if (prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2])) return false;
+    return covered_divide(e, n0, n1, n2, al, be, ga);
 }
 
 __device__ __forceinline__ float interp(float al, float be, float ga, float a, float b, float c) {
@@ -443,11 +448,10 @@ __device__ __forceinline__ void mat_words(const DgSegDev& sg, uint32_t mi, float
 }
 
 // Triangle record of an unclipped triangle (its vertices are the mesh's).
-__device__ __forceinline__ void write_record(const DgJobDev& job, const DgSegDev& sg, uint32_t t, uint4 tp,
-                                             const EdgeSet& e, const float4 r[3], uint32_t rec) {
+__device__ __forceinline__ void write_record(const DgJobDev& job, const DgSegDev& sg, uint4 tp, uint4 tuv,
+                                             uint4 tnr, const EdgeSet& e, const float4 r[3], uint32_t rec) {
     DgTriRec* R = job.trec + rec;
     store_edges(R, e);
-    const uint4 tuv = __ldg(sg.tri_uv + t), tnr = __ldg(sg.tri_nrm + t);
     const float2 u0 = __ldg(sg.uv + tuv.x), u1 = __ldg(sg.uv + tuv.y), u2 = __ldg(sg.uv + tuv.z);
     const float4 n0 = __ldg(sg.nrm + tnr.x), n1 = __ldg(sg.nrm + tnr.y), n2 = __ldg(sg.nrm + tnr.z);
     float mw[9];
@@ -466,12 +470,11 @@ __device__ __forceinline__ void write_record(const DgJobDev& job, const DgSegDev
 }
 
 // Triangle record of clip output o: attribute fields through the clip program.
-__device__ __noinline__ void write_clip_record(const DgJobDev& job, const DgSegDev& sg, uint32_t t, uint4 tp,
-                                               const EdgeSet& e, const RTri& tr, const ClipProg& P, int o,
+__device__ __noinline__ void write_clip_record(const DgJobDev& job, const DgSegDev& sg, uint4 tp, uint4 tuv,
+                                               uint4 tnr, const EdgeSet& e, const RTri& tr, const ClipProg& P, int o,
                                                uint32_t row0, uint32_t rec) {
     DgTriRec* R = job.trec + rec;
     store_edges(R, e);
-    const uint4 tuv = __ldg(sg.tri_uv + t), tnr = __ldg(sg.tri_nrm + t);
     const float2 u0 = __ldg(sg.uv + tuv.x), u1 = __ldg(sg.uv + tuv.y), u2 = __ldg(sg.uv + tuv.z);
     const float4 n0 = __ldg(sg.nrm + tnr.x), n1 = __ldg(sg.nrm + tnr.y), n2 = __ldg(sg.nrm + tnr.z);
     float mw[9];
@@ -574,78 +577,27 @@ __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
     }
 }
 
-// Rasterizes the triangles held by the lanes of a warp: the pixels of all
-// bounding boxes are numbered with an inclusive warp scan and processed 32 at
-// a time, each lane fetching its triangle's edge constants from the owner lane.
-__device__ __forceinline__ void warp_flat_raster(const DgJobDev& job, const RTri& t, const EdgeSet& e, uint32_t npx) {
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t incl = npx;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(FULL, incl, o);
-        if (lane >= (uint32_t)o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
-    const uint32_t excl = incl - npx;
-    const uint32_t w = t.xhi - t.xlo + 1u;
-    for (uint32_t base = 0; base < total; base += 32u) {
-        uint32_t j = base + lane;
-        int lo = 0, hi = 31;
-#pragma unroll
-        for (int it = 0; it < 5; it++) {
-            int mid = (lo + hi) >> 1;
-            uint32_t v = __shfl_sync(FULL, incl, mid);
-            if (v > j)
-                hi = mid;
-            else
-                lo = mid + 1;
+// Rasterizes a triangle's clipped bounding box on the calling lane alone, row
+// by row (the pixel position advances without division).
+__device__ __forceinline__ void raster_box(const EdgeSet& e, float da, float db, float dc, uint32_t seq, uint32_t xlo,
+                                           uint32_t ylo, uint32_t w, uint32_t h, const DgFrameDev& fr) {
+    unsigned long long* vis = reinterpret_cast<unsigned long long*>(fr.vis);
+    const float clear_depth = fr.clear_depth;
+    const uint32_t width = fr.width;
+    uint32_t x = xlo, y = ylo;
+    const uint32_t xe = xlo + w;
+    const uint64_t n = (uint64_t)w * h;
+    for (uint64_t k = 0; k < n; k++) {
+        float al, be, ga;
+        if (covered(e, (float)x, (float)y, al, be, ga)) {
+            const float depth = interp(al, be, ga, da, db, dc);
+            if (depth < clear_depth) atomicMin(vis + (uint64_t)y * width + x, depth_key(depth, seq));
         }
-        const int owner = lo;
-        EdgeSet oe;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            oe.A[k] = __shfl_sync(FULL, e.A[k], owner);
-            oe.B[k] = __shfl_sync(FULL, e.B[k], owner);
-            oe.C[k] = __shfl_sync(FULL, e.C[k], owner);
-            oe.D[k] = __shfl_sync(FULL, e.D[k], owner);
-            oe.den[k] = __shfl_sync(FULL, e.den[k], owner);
-        }
-        oe.tie = __shfl_sync(FULL, e.tie, owner);
-        float da = __shfl_sync(FULL, t.da, owner);
-        float db = __shfl_sync(FULL, t.db, owner);
-        float dc = __shfl_sync(FULL, t.dc, owner);
-        uint32_t seq = __shfl_sync(FULL, t.seq, owner);
-        uint32_t xlo = __shfl_sync(FULL, t.xlo, owner);
-        uint32_t ylo = __shfl_sync(FULL, t.ylo, owner);
-        uint32_t ow = __shfl_sync(FULL, w, owner);
-        uint32_t ofr = __shfl_sync(FULL, t.frame, owner);
-        uint32_t oex = __shfl_sync(FULL, excl, owner);
-        if (j < total) {
-            uint32_t k = j - oex;
-            uint32_t yy = k / ow;
-            uint32_t xx = k - yy * ow;
-            raster_pixel(oe, da, db, dc, seq, xlo + xx, ylo + yy, job.frames[ofr]);
+        if (++x == xe) {
+            x = xlo;
+            y++;
         }
     }
-}
-
-// Hands out n consecutive slots of counter c to every lane of the warp with one
-// atomic; returns this lane's first slot.
-__device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* c, uint32_t n) {
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t incl = n;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t v = __shfl_up_sync(FULL, incl, o);
-        if (lane >= (uint32_t)o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
-    unsigned long long old = 0;
-    if (total != 0u) {
-        if (lane == 0u) old = atomicAdd(c, (unsigned long long)total);
-        old = __shfl_sync(FULL, old, 0);
-    }
-    return old + (incl - n);
 }
 
 // Setup pass over the cull survivors (dense, one per thread): near/far
@@ -662,7 +614,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
         const uint32_t i = base + lane;
         int nout = 0;
         uint32_t g = 0, si = 0, t = 0, row0 = 0, nrows = 0;
-        uint4 tp = make_uint4(0, 0, 0, 0);
+        uint4 tp = make_uint4(0, 0, 0, 0), tuv = tp, tnr = tp;
         float4 r[3];
         bool clipped = false;
         if (i < nsurv) {
@@ -671,6 +623,8 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             const DgSegDev& sg = job.segs[si];
             t = g - sg.tri_begin;
             tp = __ldg(sg.tri_pos + t);
+            tuv = __ldg(sg.tri_uv + t);  // for the triangle record, loaded alongside the vertex records
+            tnr = __ldg(sg.tri_nrm + t);
             r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
             r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
             r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
@@ -701,10 +655,19 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                 for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
             }
         }
-        // consecutive records for the clip outputs of each triangle
-        const unsigned long long rb = warp_alloc(job.cnt + DG_CNT_TREC, (uint32_t)nout);
+        // Triangle records: a triangle with one output uses record i (its survivor
+        // slot); the clip outputs of one with more take consecutive records after
+        // the first total_tri.
         uint32_t rbase = DG_NONE;
-        if (nout > 0 && nrows != DG_NONE && rb + (unsigned long long)nout <= job.trec_cap) rbase = (uint32_t)rb;
+        if (nout == 1 && nrows != DG_NONE) {
+            if (i < job.trec_cap) rbase = i;
+        } else if (nout > 1 && nrows != DG_NONE) {
+            const unsigned long long rb =
+                (unsigned long long)job.total_tri + atomicAdd(job.cnt + DG_CNT_TRECX, (unsigned long long)nout);
+            if (rb + (unsigned long long)nout <= job.trec_cap) rbase = (uint32_t)rb;
+        }
+        const uint32_t nrec = __reduce_add_sync(FULL, (uint32_t)nout);
+        if (lane == 0u && nrec) atomicAdd(job.cnt + DG_CNT_TREC, (unsigned long long)nrec);  // statistics only
         if (i < nsurv) job.rec_of[g] = rbase;
 
         for (int rr = 0;; rr++) {
@@ -712,9 +675,9 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             if (__ballot_sync(FULL, has) == 0u) break;
             RTri tr;
             EdgeSet e;
-            uint32_t npx = 0;
+            bool small = false;  // goes to the small-triangle list
             uint32_t nu = 0;     // work units to queue (0: not queued)
-            uint64_t qpx = 0;    // bounding-box pixels of the queued triangle
+            uint32_t qpx = 0;    // bounding-box pixels of the queued triangle
             bool inplace = false;
             tr.xlo = tr.xhi = tr.ylo = tr.yhi = 0;
             tr.frame = 0;
@@ -742,17 +705,17 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                     make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
                     if (rbase != DG_NONE) {
                         if (!clipped)
-                            write_record(job, sg, t, tp, e, r, rbase);
+                            write_record(job, sg, tp, tuv, tnr, e, r, rbase);
                         else
-                            write_clip_record(job, sg, t, tp, e, tr, P, rr, row0, rbase + (uint32_t)rr);
+                            write_clip_record(job, sg, tp, tuv, tnr, e, tr, P, rr, row0, rbase + (uint32_t)rr);
                     }
                     uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
-                    if (px <= job.small_max_px) {
-                        npx = (uint32_t)px;
-                    } else if (rbase == DG_NONE) {
+                    if (rbase == DG_NONE) {
                         inplace = true;
+                    } else if (px <= job.small_max_px) {
+                        small = true;
                     } else {
-                        qpx = px;
+                        qpx = (uint32_t)px;  // below 2^31: the canvas has fewer pixels
                         nu = (uint32_t)((px + DG_UNIT_PX - 1u) / DG_UNIT_PX);
                     }
                 }
@@ -762,7 +725,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             // items, each lane taking every 32nd.
             const unsigned qmask = __ballot_sync(FULL, nu != 0u);
             if (qmask) {
-                const uint32_t ni = (nu + DG_ITEM_UNITS - 1u) / DG_ITEM_UNITS;
+                const uint32_t ni = (nu + job.item_units - 1u) / job.item_units;
                 uint32_t incl = ni, uincl = nu;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
@@ -789,51 +752,105 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                 if (fits) {
                     uint4* qd = reinterpret_cast<uint4*>(job.queue + rec);
                     qd[0] = make_uint4(rbase + (uint32_t)rr, tr.seq, tr.frame, tr.xlo);
-                    qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, (uint32_t)qpx, nu);
+                    qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, qpx, nu);
                 } else if (nu != 0u) {
                     inplace = true;  // queue full: this lane rasterizes the box itself
                 }
-                // items of all lanes: item j belongs to the first lane whose inclusive count exceeds it
-                const uint32_t excl = incl - ni;
-                for (uint32_t b0 = 0; b0 < total_items; b0 += 32u) {
+                // Items of a lane that did not fit are marked empty (their slots are handed out).
+                // Lanes with at least 32 items: the whole warp writes them, one lane after another.
+                unsigned big = __ballot_sync(FULL, ni >= 32u);
+                while (big) {
+                    const int L = __ffs(big) - 1;
+                    big &= big - 1u;
+                    const uint32_t lni = __shfl_sync(FULL, ni, L);
+                    const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, L);
+                    const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, L);
+                    const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, L) != 0u;
+                    for (uint32_t k = lane; k < lni; k += 32u)
+                        if (oib + k < job.items_cap)
+                            job.items[oib + k] = ofits ? make_uint2(orec, k * job.item_units) : make_uint2(DG_NONE, 0u);
+                }
+                // The other lanes' items numbered together: item j belongs to the first lane
+                // whose inclusive count exceeds it.
+                const uint32_t ns = ni < 32u ? ni : 0u;
+                uint32_t sincl = ns;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_up_sync(FULL, sincl, o);
+                    if (lane >= (uint32_t)o) sincl += v;
+                }
+                const uint32_t stotal = __shfl_sync(FULL, sincl, 31);
+                const uint32_t sexcl = sincl - ns;
+                for (uint32_t b0 = 0; b0 < stotal; b0 += 32u) {
                     const uint32_t j = b0 + lane;
                     int lo = 0, hi = 31;
 #pragma unroll
                     for (int it = 0; it < 5; it++) {
                         const int mid = (lo + hi) >> 1;
-                        if (__shfl_sync(FULL, incl, mid) > j)
+                        if (__shfl_sync(FULL, sincl, mid) > j)
                             hi = mid;
                         else
                             lo = mid + 1;
                     }
                     const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, lo);
                     const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, lo);
-                    const uint32_t oex = __shfl_sync(FULL, excl, lo);
+                    const uint32_t oex = __shfl_sync(FULL, sexcl, lo);
                     const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, lo) != 0u;
                     const uint32_t k = j - oex;  // item index within its record
-                    // items of a lane that did not fit are marked empty (the slots are handed out)
-                    if (j < total_items && oib + k < job.items_cap)
-                        job.items[oib + k] = ofits ? make_uint2(orec, k * DG_ITEM_UNITS) : make_uint2(DG_NONE, 0u);
+                    if (j < stotal && oib + k < job.items_cap)
+                        job.items[oib + k] = ofits ? make_uint2(orec, k * job.item_units) : make_uint2(DG_NONE, 0u);
+                }
+            }
+            // Small triangles go to the small-triangle list (one atomic per warp), which the
+            // queue pass rasterizes one triangle per lane.
+            const unsigned smask = __ballot_sync(FULL, small);
+            if (smask) {
+                const int leader = __ffs(smask) - 1;
+                unsigned long long old = 0;
+                if ((int)lane == leader) old = atomicAdd(job.cnt + DG_CNT_SMALL, (unsigned long long)__popc(smask));
+                old = __shfl_sync(FULL, old, leader);
+                const uint64_t slot = old + __popc(smask & ((1u << lane) - 1u));
+                if (small) {
+                    if (slot < job.small_cap) {
+                        uint4* qd = reinterpret_cast<uint4*>(job.small + slot);
+                        qd[0] = make_uint4(rbase + (uint32_t)rr, tr.seq, tr.frame, tr.xlo);
+                        qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, tr.yhi - tr.ylo + 1u, 0u);
+                    } else {
+                        inplace = true;  // list full
+                    }
                 }
             }
             if (inplace) {  // this lane rasterizes the box itself
                 atomicAdd(job.cnt + DG_CNT_INPLACE, 1ull);
-                const DgFrameDev& fr = job.frames[tr.frame];
-                for (uint32_t y = tr.ylo; y <= tr.yhi; y++)
-                    for (uint32_t x = tr.xlo; x <= tr.xhi; x++)
-                        raster_pixel(e, tr.da, tr.db, tr.dc, tr.seq, x, y, fr);
+                raster_box(e, tr.da, tr.db, tr.dc, tr.seq, tr.xlo, tr.ylo, tr.xhi - tr.xlo + 1u, tr.yhi - tr.ylo + 1u,
+                           job.frames[tr.frame]);
             }
-            warp_flat_raster(job, tr, e, npx);
         }
     }
 }
 
 // The raster queue: the bounding-box pixels of every queued triangle in
 // row-major units of DG_UNIT_PX (one pixel per lane), grouped into work items
-// of at most DG_ITEM_UNITS units that the warps take in a strided order.
+// of at most job.item_units units that the warps take in a strided order.
+// One candidate fragment of a queued triangle (its pixel passed prereject):
+// the coverage test with the divisions, the depth, the strict test against the
+// clear depth and the keyed minimum.
+__device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uint32_t seq, uint32_t x, uint32_t y,
+                                                float clear_depth, unsigned long long* vis, uint32_t width) {
+    float al, be, ga;
+    const float xf = (float)x, yf = (float)y;
+    if (covered_divide(e, edge_eval(e, 0, xf, yf), edge_eval(e, 1, xf, yf), edge_eval(e, 2, xf, yf), al, be, ga)) {
+        const float depth = interp(al, be, ga, dd.x, dd.y, dd.z);
+        if (depth < clear_depth) atomicMin(vis + (uint64_t)y * width + x, depth_key(depth, seq));
+    }
+}
+
 __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
+    __shared__ uint32_t s_bx[8][64], s_by[8][64];  // per-warp candidate buffers
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
+    uint32_t* bx = s_bx[threadIdx.x >> 5];
+    uint32_t* by = s_by[threadIdx.x >> 5];
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     // Prologue: light/halfway vectors of the vertices the setup pass marked, one
@@ -848,7 +865,25 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
     const unsigned long long cnt = __ldcg(job.cnt + DG_CNT_QUEUE);
     const uint64_t ni64 = cnt & ((1ull << DG_PACK_SHIFT) - 1ull);
     const uint32_t nitems = (uint32_t)(ni64 < job.items_cap ? ni64 : job.items_cap);
-    for (uint32_t it = warp; it < nitems; it += nwarps) {
+    const unsigned long long ns64 = __ldcg(job.cnt + DG_CNT_SMALL);
+    const uint32_t nsmall = (uint32_t)(ns64 < job.small_cap ? ns64 : job.small_cap);
+    const uint32_t nchunks = (nsmall + 31u) >> 5;
+    // Work index wi: chunks of 32 small triangles first (wi < nchunks), then the work items.
+    for (uint32_t wi = warp; wi < nchunks + nitems; wi += nwarps) {
+        if (wi < nchunks) {  // one small triangle per lane, rasterized by that lane
+            const uint32_t i = (wi << 5) + lane;
+            if (i < nsmall) {
+                const uint4* qs = reinterpret_cast<const uint4*>(job.small + i);
+                const uint4 q0 = __ldcg(qs), q1 = __ldcg(qs + 1);
+                const DgTriRec* R = job.trec + q0.x;
+                EdgeSet e;
+                load_edges(R, e);
+                const float4 dd = __ldg(reinterpret_cast<const float4*>(R) + 4);
+                raster_box(e, dd.x, dd.y, dd.z, q0.y, q0.w, q1.x, q1.y, q1.z, job.frames[q0.z]);
+            }
+            continue;
+        }
+        const uint32_t it = wi - nchunks;
         const uint2 item = __ldcg(job.items + it);
         if (item.x >= job.queue_cap) continue;  // an item of a triangle that did not fit the queue
         const uint4* qs = reinterpret_cast<const uint4*>(job.queue + item.x);
@@ -864,22 +899,50 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
         const uint32_t width = fr.width;
         const uint32_t xlo = q0.w, ylo = q1.x, w = q1.y, npx = q1.z;
         const float rcp_w = __frcp_rn((float)w);
-        const uint32_t u_end = min(q1.w, item.y + DG_ITEM_UNITS);
+        const uint32_t u_end = min(q1.w, item.y + job.item_units);
+        // Stage A: every lane takes one pixel of the unit and applies the exact,
+        // division-free pre-reject; candidates are packed into the warp's buffer.
+        // Stage B: whenever 32 candidates are buffered, each lane finishes one of
+        // them (the reference's full test with its three divisions, then the
+        // depth key), so the division path runs with all lanes busy.
+        uint32_t pending = 0;
         for (uint32_t u = item.y; u < u_end; u++) {
             const uint32_t k = u * DG_UNIT_PX + lane;
+            bool cand = false;
+            uint32_t x = 0, y = 0;
             if (k < npx) {
                 // k / w from a float reciprocal, corrected to the exact quotient
                 uint32_t yy = (uint32_t)__fmul_rz((float)k, rcp_w);
                 while ((uint64_t)yy * w > k) yy--;
                 while ((uint64_t)(yy + 1u) * w <= k) yy++;
-                const uint32_t x = xlo + (k - yy * w), y = ylo + yy;
-                float al, be, ga;
-                if (covered(e, (float)x, (float)y, al, be, ga)) {
-                    const float depth = interp(al, be, ga, dd.x, dd.y, dd.z);
-                    if (depth < clear_depth) atomicMin(vis + (uint64_t)y * width + x, depth_key(depth, seq));
+                x = xlo + (k - yy * w);
+                y = ylo + yy;
+                const float xf = (float)x, yf = (float)y;
+                cand = !(prereject(edge_eval(e, 0, xf, yf), e.den[0]) || prereject(edge_eval(e, 1, xf, yf), e.den[1]) ||
+                         prereject(edge_eval(e, 2, xf, yf), e.den[2]));
+            }
+            const unsigned b = __ballot_sync(FULL, cand);
+            if (cand) {
+                const uint32_t slot = pending + __popc(b & ((1u << lane) - 1u));
+                bx[slot] = x;
+                by[slot] = y;
+            }
+            pending += __popc(b);
+            if (pending >= 32u) {
+                __syncwarp();
+                finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width);
+                __syncwarp();
+                if (lane < pending - 32u) {
+                    bx[lane] = bx[32u + lane];
+                    by[lane] = by[32u + lane];
                 }
+                __syncwarp();
+                pending -= 32u;
             }
         }
+        __syncwarp();
+        if (lane < pending) finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width);
+        __syncwarp();
     }
 }
 
@@ -1118,47 +1181,60 @@ __device__ __noinline__ uint32_t shade_without_record(const DgJobDev& job, const
     return shade_colour(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
 }
 
-// Shade-list entry: x = job-wide pixel index, with DG_SHADE_KEY set when y holds
-// the key's low word (no triangle record) instead of the record index.
-#define DG_SHADE_KEY 0x80000000u
-
-// Resolve, pass 1 (one 32 x 32 tile per CTA, four rows per thread): an empty
-// pixel gets the clear colour and depth; a covered one has its key reset for
-// the next frame and is appended to the shade list with its triangle record
-// (one atomic per tile).
-__global__ void __launch_bounds__(256) k_resolve(const DgJobDev job) {
-    __shared__ __align__(8) uint32_t sh[12];
+// Resolve and shade, fused: one 32 x TH tile per CTA of 256 threads (TH = 8,
+// 16 or 32: the tile_rows knob).
+//  1. Each thread reads the visibility keys of TH/8 pixels (rows r, r+8, ...
+//     of its column). An empty pixel gets the clear colour and depth
+//     (this is Canvas::clear, canvas.rs:425-433); a covered one has its key
+//     reset for the next frame and goes into the tile's shade list in shared
+//     memory with its triangle record, in row-major order. A covered pixel
+//     whose triangle has no record keeps its key and the tile is listed for
+//     k_resolve_fallback.
+//  2. The CTA shades its list densely: the winning fragment of every covered
+//     pixel is shaded once (canvas.rs:682-741) and its colour (row H-1-y) and
+//     depth (y*W+x) are written (canvas.rs:923-930).
+template <uint32_t TH>
+__global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
+    __shared__ float inv255[256];
+    __shared__ DgTexDev stex[DG_SMEM_TEX];
+    __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
+    __shared__ uint32_t s_val[DG_TILE_W * TH];  // triangle record
+    __shared__ uint32_t s_row[34];  // shade-list offset of each tile row; [32] = total, [33] = pixels without record
+    // independent of the previous kernel: the quotient table and the texture descriptors
+    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
+    const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
+    for (uint32_t i = threadIdx.x; i < nst * 3u; i += blockDim.x)
+        reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
     wait_previous_kernel();
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_row[33] = 0u;
     const uint32_t tile = blockIdx.x;
     const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
     const DgFrameDev& fr = job.frames[fi];
     const uint32_t lt = tile - fr.tile_begin;
     const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
     const uint32_t x = tx * DG_TILE_W + lane;
-    const uint32_t y0 = ty * DG_TILE_H + (threadIdx.x >> 5);
     const uint32_t W = fr.width, H = fr.height;
-    constexpr int R = DG_TILE_H / 8;
+    constexpr int R = TH / 8;
     uint64_t key[R];
 #pragma unroll
-    for (int j = 0; j < R; j++) {  // all loads first: four keys in flight per thread
-        const uint32_t y = y0 + 8u * j;
+    for (int j = 0; j < R; j++) {  // all loads first: R keys in flight per thread
+        const uint32_t y = ty * TH + wid + 8u * j;
         key[j] = (x < W && y < H) ? __ldcg(reinterpret_cast<const unsigned long long*>(fr.vis) + (uint64_t)y * W + x)
                                   : DG_VIS_EMPTY - 1ull;  // outside the canvas
     }
     uint32_t val[R];
-    uint32_t nhit = 0;
+    unsigned hit[R];
 #pragma unroll
     for (int j = 0; j < R; j++) {
-        const uint32_t y = y0 + 8u * j;
+        const uint32_t y = ty * TH + wid + 8u * j;
         const uint64_t i = (uint64_t)y * W + x;
+        const bool covered_px = key[j] < DG_VIS_EMPTY - 1ull;
         val[j] = DG_NONE;
         if (key[j] == DG_VIS_EMPTY) {
             fr.depth[i] = fr.clear_depth;
             fr.colour[(uint64_t)(H - 1u - y) * W + x] = AZUL_BB;
-        } else if (key[j] < DG_VIS_EMPTY - 1ull) {
-            fr.vis[i] = DG_VIS_EMPTY;
-            nhit++;
+        } else if (covered_px) {
             // the triangle record of the key: segment of the submission index, then rec_of
             const uint32_t seq = (uint32_t)key[j];
             const uint32_t tl = seq >> 2;
@@ -1168,85 +1244,114 @@ __global__ void __launch_bounds__(256) k_resolve(const DgJobDev job) {
             const DgSegDev& sg = job.segs[si];
             const uint32_t t = tl - sg.seq_base;
             if (t < sg.ntri) val[j] = __ldg(job.rec_of + sg.tri_begin + t);
+            const uint32_t o = (uint32_t)key[j] & 3u;
+            if (val[j] != DG_NONE && (uint64_t)val[j] + o < job.trec_cap) {
+                val[j] += o;
+                fr.vis[i] = DG_VIS_EMPTY;
+            } else {
+                val[j] = DG_NONE;  // shaded by the fallback pass, which resets the key
+                s_row[33] = 1u;
+            }
         }
+        hit[j] = __ballot_sync(FULL, covered_px && val[j] != DG_NONE);
+        if (lane == 0) s_row[wid + 8u * j] = __popc(hit[j]);
     }
-    // one atomic per tile for the shade-list slots of its covered pixels
-    const uint32_t wid = threadIdx.x >> 5;
-    uint32_t incl = nhit;
+    __syncthreads();
+    if (wid == 0) {  // exclusive scan of the TH row counts
+        const uint32_t c = lane < TH ? s_row[lane] : 0u;
+        uint32_t incl = c;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(FULL, incl, o);
-        if (lane >= (uint32_t)o) incl += v;
-    }
-    if (lane == 31u) sh[wid] = incl;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (uint32_t w = 0; w < 8u; w++) {
-            const uint32_t k = sh[w];
-            sh[w] = run;
-            run += k;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
         }
-        *reinterpret_cast<unsigned long long*>(sh + 10) =
-            run ? atomicAdd(job.cnt + DG_CNT_COVERED, (unsigned long long)run) : 0ull;
+        s_row[lane] = incl - c;
+        if (lane == 31u) {
+            s_row[32] = incl;
+            if (incl) atomicAdd(job.cnt + DG_CNT_COVERED, (unsigned long long)incl);
+        }
     }
     __syncthreads();
-    unsigned long long slot = *reinterpret_cast<unsigned long long*>(sh + 10) + sh[wid] + (incl - nhit);
 #pragma unroll
     for (int j = 0; j < R; j++) {
-        if (key[j] < DG_VIS_EMPTY - 1ull) {
-            const uint32_t y = y0 + 8u * j;
-            const uint32_t p = fr.pix_begin + (uint32_t)((uint64_t)y * W + x);
-            const uint32_t seq = (uint32_t)key[j];
-            uint2 ent;
-            if (val[j] != DG_NONE && (uint64_t)val[j] + (seq & 3u) < job.trec_cap)
-                ent = make_uint2(p, val[j] + (seq & 3u));
-            else
-                ent = make_uint2(p | DG_SHADE_KEY, seq);
-            if (slot < job.total_px) job.shade_list[slot] = ent;
-            slot++;
+        if ((hit[j] >> lane) & 1u) {
+            const uint32_t row = wid + 8u * j;
+            const uint32_t slot = s_row[row] + __popc(hit[j] & ((1u << lane) - 1u));
+            s_pix[slot] = (uint16_t)(row * DG_TILE_W + lane);
+            s_val[slot] = val[j];
         }
     }
-}
-
-// Resolve, pass 2: the winning fragment of every covered pixel is shaded once
-// (canvas.rs:682-741) and its colour (row H-1-y) and depth (y*W+x) are written
-// (canvas.rs:923-930). Dense over the shade list.
-__global__ void __launch_bounds__(256, 4) k_shade(const DgJobDev job) {
-    __shared__ float inv255[256];
-    __shared__ DgTexDev stex[DG_SMEM_TEX];
-    // independent of the previous kernel: the quotient table and the texture descriptors
-    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
-    const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
-    for (uint32_t i = threadIdx.x; i < nst * 3u; i += blockDim.x)
-        reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
-    wait_previous_kernel();
     __syncthreads();
-    const unsigned long long n64 = __ldcg(job.cnt + DG_CNT_COVERED);
-    const uint32_t n = (uint32_t)(n64 < job.total_px ? n64 : job.total_px);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-        const uint2 ent = __ldcg(job.shade_list + k);
-        const uint32_t p = ent.x & ~DG_SHADE_KEY;
-        const uint32_t fi = last_le(job.nframes, p, [&](uint32_t i) { return job.frames[i].pix_begin; });
-        const DgFrameDev& fr = job.frames[fi];
-        const uint32_t local = p - fr.pix_begin;
-        const uint32_t y = local / fr.width, x = local - y * fr.width;
+    const uint32_t n = s_row[32];
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const uint32_t pe = s_pix[k];
+        const uint32_t px = tx * DG_TILE_W + (pe & 31u), py = ty * TH + (pe >> 5);
         float d = 0.0f;
         int errc;
-        uint32_t c;
-        if (ent.x & DG_SHADE_KEY)
-            c = shade_without_record(job, fr, ent.y, x, y, inv255, stex, d, errc);
-        else
-            c = shade_from_record(job, fr, job.trec + ent.y, x, y, inv255, stex, d, errc);
+        uint32_t c = shade_from_record(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc);
         if (errc != DG_OK) c = AZUL_BB;
         // one error-word update per warp (every pixel of a bad job may fail)
         const unsigned act = __activemask();
         const uint32_t bits = __reduce_or_sync(act, errc != DG_OK ? 1u << errc : 0u);
-        if (bits != 0u && (threadIdx.x & 31u) == (uint32_t)(__ffs(act) - 1)) atomicOr(job.err, bits);
-        fr.depth[local] = d;
-        fr.colour[(uint64_t)(fr.height - 1u - y) * fr.width + x] = c;
+        if (bits != 0u && lane == (uint32_t)(__ffs(act) - 1)) atomicOr(job.err, bits);
+        fr.depth[(uint64_t)py * W + px] = d;
+        fr.colour[(uint64_t)(H - 1u - py) * W + px] = c;
     }
+    // a tile with pixels whose triangle has no record goes to the fallback pass
+    if (threadIdx.x == 0 && s_row[33] != 0u) {
+        const unsigned long long slot = atomicAdd(job.cnt + DG_CNT_FBTILES, 1ull);
+        if (slot < job.total_tiles) job.fb_tiles[slot] = tile;
+    }
+}
+
+// Fallback pass of the resolve: pixels whose winning triangle has no record (the
+// record buffers were full) kept their keys in k_resolve; here the tiles that
+// hold such pixels are read again and those pixels are shaded from the mesh
+// (shade_without_record) and their keys reset. Exits at once when no tile
+// needs it.
+template <uint32_t TH>
+__global__ void __launch_bounds__(256) k_resolve_fallback(const DgJobDev job) {
+    __shared__ float inv255[256];
+    __shared__ DgTexDev stex[DG_SMEM_TEX];
+    wait_previous_kernel();
+    const unsigned long long n64 = __ldcg(job.cnt + DG_CNT_FBTILES);
+    const uint32_t ntiles = (uint32_t)(n64 < job.total_tiles ? n64 : job.total_tiles);
+    if (ntiles == 0u) return;
+    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
+    const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
+    for (uint32_t i = threadIdx.x; i < nst * 3u; i += blockDim.x)
+        reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    uint32_t shaded = 0;
+    for (uint32_t ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+        const uint32_t tile = __ldcg(job.fb_tiles + ti);
+        const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
+        const DgFrameDev& fr = job.frames[fi];
+        const uint32_t lt = tile - fr.tile_begin;
+        const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
+        const uint32_t x = tx * DG_TILE_W + lane;
+        const uint32_t W = fr.width, H = fr.height;
+        for (uint32_t j = 0; j < TH / 8u; j++) {
+            const uint32_t y = ty * TH + wid + 8u * j;
+            if (x >= W || y >= H) continue;
+            const uint64_t i = (uint64_t)y * W + x;
+            const uint64_t key = __ldcg(reinterpret_cast<const unsigned long long*>(fr.vis) + i);
+            if (key == DG_VIS_EMPTY) continue;  // empty, or shaded by k_resolve
+            fr.vis[i] = DG_VIS_EMPTY;
+            float d = 0.0f;
+            int errc;
+            uint32_t c = shade_without_record(job, fr, (uint32_t)key, x, y, inv255, stex, d, errc);
+            if (errc != DG_OK) {
+                c = AZUL_BB;
+                atomicOr(job.err, 1u << errc);
+            }
+            fr.depth[i] = d;
+            fr.colour[(uint64_t)(H - 1u - y) * W + x] = c;
+            shaded++;
+        }
+    }
+    if (shaded) atomicAdd(job.cnt + DG_CNT_COVERED, (unsigned long long)shaded);
 }
 
 __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, float dv, int fc, int fd) {
@@ -1312,14 +1417,14 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
     }
     if ((e = mark(4)) != cudaSuccess) return e;
     if (job.total_tiles) {
-        if ((e = launch_dependent(k_resolve, job.total_tiles, 256, job, s)) != cudaSuccess) return e;
+        auto kr = job.tile_rows == 8u ? k_resolve<8> : job.tile_rows == 16u ? k_resolve<16> : k_resolve<32>;
+        if ((e = launch_dependent(kr, job.total_tiles, 256, job, s)) != cudaSuccess) return e;
+        auto kf = job.tile_rows == 8u    ? k_resolve_fallback<8>
+                  : job.tile_rows == 16u ? k_resolve_fallback<16>
+                                         : k_resolve_fallback<32>;
+        if ((e = launch_dependent(kf, cfg.fallback_blocks, 256, job, s)) != cudaSuccess) return e;
     }
-    if ((e = mark(5)) != cudaSuccess) return e;
-    if (job.total_px) {
-        const unsigned hb = cfg.shade_blocks < 1u ? 1u : cfg.shade_blocks;
-        if ((e = launch_dependent(k_shade, grid_for(job.total_px, hb), 256, job, s)) != cudaSuccess) return e;
-    }
-    return mark(6);
+    return mark(5);
 }
 
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,

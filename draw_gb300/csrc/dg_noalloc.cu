@@ -31,18 +31,20 @@ struct NoallocDesc {  // the job descriptor the kernels read
 };
 constexpr size_t kOffDesc = 0;
 constexpr uint32_t kVrowExtra = 4096;  // light/halfway rows for clip vertices
-constexpr uint32_t kTrecCap = DG_NOALLOC_MAX_TRIANGLES + 4096;  // triangle records
+constexpr uint32_t kTrecCap = (uint32_t)dg_trec_cap(DG_NOALLOC_MAX_TRIANGLES);  // triangle records
 constexpr size_t kOffVrec = align_up(kOffDesc + sizeof(NoallocDesc));
 constexpr size_t kOffVshade = align_up(kOffVrec + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(float4));
 constexpr size_t kOffVmark = align_up(kOffVshade + (size_t)(DG_NOALLOC_MAX_VERTICES + kVrowExtra) *
                                                        DG_NOALLOC_MAX_LIGHTS * 2 * sizeof(float4));
 constexpr size_t kOffQueue = align_up(kOffVmark + (size_t)(DG_NOALLOC_MAX_VERTICES / 32) * sizeof(uint32_t));
-constexpr size_t kOffQbase = align_up(kOffQueue + (size_t)kQueueCap * sizeof(DgQueueRec));
+constexpr size_t kOffSmall = align_up(kOffQueue + (size_t)kQueueCap * sizeof(DgQueueRec));
+constexpr size_t kOffQbase = align_up(kOffSmall + (size_t)kQueueCap * sizeof(DgQueueRec));
 constexpr size_t kOffSurv = align_up(kOffQbase + (size_t)dg_items_cap(kQueueCap) * sizeof(uint2));
 constexpr size_t kOffRecOf = align_up(kOffSurv + (size_t)DG_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t));
 constexpr size_t kOffTrec = align_up(kOffRecOf + (size_t)DG_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t));
-constexpr size_t kOffShade = align_up(kOffTrec + (size_t)kTrecCap * sizeof(DgTriRec));
-constexpr size_t kOffCounters = align_up(kOffShade + (size_t)DG_NOALLOC_MAX_PIXELS * sizeof(uint2));
+constexpr uint32_t kFbCap = 16384;  // resolve fallback tiles: more than a canvas within the pixel limit has
+constexpr size_t kOffFb = align_up(kOffTrec + (size_t)kTrecCap * sizeof(DgTriRec));
+constexpr size_t kOffCounters = align_up(kOffFb + (size_t)kFbCap * sizeof(uint32_t));
 constexpr size_t kOffErr = align_up(kOffCounters + DG_NCOUNTERS * sizeof(unsigned long long));
 constexpr size_t kOffWhite = align_up(kOffErr + sizeof(uint32_t));
 constexpr size_t kOffVis = align_up(kOffWhite + 8);
@@ -143,6 +145,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     f.tiles_x = (p->canvas_width + DG_TILE_W - 1) / DG_TILE_W;
     f.pix_begin = 0;
     const uint32_t tiles = f.tiles_x * ((p->canvas_height + DG_TILE_H - 1) / DG_TILE_H);
+    if (tiles > kFbCap) return DG_E_LIMIT;  // not reachable within DG_NOALLOC_MAX_PIXELS
 
     DgSegDev& sg = d.seg;
     sg.frame = 0;
@@ -196,6 +199,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.total_vtx = m->nv;
     job.total_tri = m->ntri;
     job.total_tiles = tiles;
+    job.fb_tiles = reinterpret_cast<uint32_t*>(base + kOffFb);
     job.shade_stride = p->nlights;
     job.vrec = reinterpret_cast<float4*>(base + kOffVrec);
     job.vshade = reinterpret_cast<float4*>(base + kOffVshade);
@@ -206,13 +210,16 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.trec = reinterpret_cast<DgTriRec*>(base + kOffTrec);
     job.trec_cap = kTrecCap;
     job.queue = reinterpret_cast<DgQueueRec*>(base + kOffQueue);
+    job.small = reinterpret_cast<DgQueueRec*>(base + kOffSmall);
+    job.small_cap = kQueueCap;
     job.items = reinterpret_cast<uint2*>(base + kOffQbase);
     job.items_cap = (uint32_t)dg_items_cap(kQueueCap);
     job.queue_cap = kQueueCap;
     job.small_max_px = DG_SMALL_MAX_PX;
+    job.item_units = DG_ITEM_UNITS;
     job.cnt = reinterpret_cast<unsigned long long*>(base + kOffCounters);
     job.total_px = (uint32_t)npx;
-    job.shade_list = reinterpret_cast<uint2*>(base + kOffShade);
+    job.tile_rows = DG_TILE_H;
     job.tex = reinterpret_cast<const DgTexDev*>(base + kOffDesc + offsetof(NoallocDesc, tex));
     job.ntex = ntex + 1;
     job.err = reinterpret_cast<uint32_t*>(base + kOffErr);
@@ -234,7 +241,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     cfg.cull_blocks = (unsigned)nsm * DG_CULL_BLOCKS_PER_SM;
     cfg.setup_blocks = (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM;
     cfg.queue_blocks = (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM;
-    cfg.shade_blocks = (unsigned)nsm * DG_SHADE_BLOCKS_PER_SM;
+    cfg.fallback_blocks = (unsigned)nsm;
     NA_CUDA(dg_launch_job(job, cfg, s, nullptr));
 
     if (status_out) {

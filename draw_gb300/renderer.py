@@ -65,6 +65,11 @@ SIGNATURES = {
     "dg_scene_render": (_i32, [_P, _i32, _i32]),
     "dg_render_batch": (_i32, [_P, _P, _P, _u32]),
     "dg_render_noalloc": (_i32, [_P, _P, _P, _u32, _P, _u32, _P, _P, _P, _P]),
+    "dg_batch_create": (_i32, [_P, _P, _P, _u32, _P]),
+    "dg_batch_render": (_i32, [_P]),
+    "dg_batch_info": (_i32, [_P, _P, _i32]),
+    "dg_batch_destroy": (_i32, [_P]),
+    "dg_autotune": (_i32, [_P, _P, _P, _u32, _u32, _P, _P]),
     "dg_server_create": (_i32, [_P, _u64, _u32, _u32, _P]),
     "dg_server_submit": (_i32, [_P, _P, _P]),
     "dg_server_wait": (_i32, [_P, _u64, _P, _P, _P]),
@@ -144,12 +149,13 @@ def load_library() -> ctypes.CDLL:
 
 
 # Kernels of one render job in launch order (dg_ctx_kernel_times).
-KERNELS = ["vertex", "cull", "setup_raster", "queue_raster", "resolve", "shade"]
+KERNELS = ["vertex", "cull", "setup_raster", "queue_raster", "resolve"]
 # dg_tuning fields in order.
-TUNING_KEYS = ["small_max_px", "setup_blocks_per_sm", "queue_blocks_per_sm", "cull_blocks_per_sm", "record_limit"]
+TUNING_KEYS = ["small_max_px", "setup_blocks_per_sm", "queue_blocks_per_sm", "cull_blocks_per_sm", "record_limit",
+               "tile_rows", "item_units"]
 # dg_ctx_last_stats entries in order.
 STATS_KEYS = ["vertices", "triangles", "queued_triangles", "queued_units", "covered_pixels", "inplace_triangles",
-              "h2d_bytes", "launches", "survivors", "triangle_records", "clip_rows"]
+              "h2d_bytes", "launches", "survivors", "triangle_records", "clip_rows", "small_triangles"]
 
 
 def _chk(st: int, what: str):
@@ -222,6 +228,56 @@ class Context:
         s = np.array([x.id for x in scenes], np.int32)
         c = np.array([x.id for x in canvases], np.int32)
         _chk(self.lib.dg_render_batch(self.h, _ptr(s), _ptr(c), len(scenes)), "render_batch")
+
+    def batch(self, scenes: list, canvases: list) -> "Batch":
+        """The batched form replayed from a CUDA graph (dg_batch_*)."""
+        return Batch(self, scenes, canvases)
+
+    def autotune(self, scenes: list, canvases: list, reps: int = 3) -> tuple[dict, float]:
+        """dg_autotune over these frames: sets and returns the fastest tuning and its ms per render."""
+        s = np.array([x.id for x in scenes], np.int32)
+        c = np.array([x.id for x in canvases], np.int32)
+        raw = (ctypes.c_uint32 * len(TUNING_KEYS))()
+        ms = ctypes.c_float()
+        _chk(self.lib.dg_autotune(self.h, _ptr(s), _ptr(c), len(scenes), int(reps), raw, ctypes.byref(ms)),
+             "autotune")
+        return dict(zip(TUNING_KEYS, list(raw))), float(ms.value)
+
+
+BATCH_INFO_KEYS = ["frames", "captures", "replays", "kernels_per_replay", "h2d_bytes_per_replay"]
+
+
+class Batch:
+    """n (scene, canvas) frames rendered as one job whose launch sequence is a
+    CUDA graph captured once and replayed by each render() (dg_batch_render).
+    Cameras and lights may change between renders; shape changes re-capture."""
+
+    def __init__(self, ctx: Context, scenes: list, canvases: list):
+        self.ctx = ctx
+        s = np.array([x.id for x in scenes], np.int32)
+        c = np.array([x.id for x in canvases], np.int32)
+        h = ctypes.c_void_p()
+        _chk(ctx.lib.dg_batch_create(ctx.h, _ptr(s), _ptr(c), len(scenes), ctypes.byref(h)), "batch_create")
+        self.h = h
+
+    def render(self):
+        _chk(self.ctx.lib.dg_batch_render(self.h), "batch_render")
+
+    def info(self) -> dict:
+        v = (ctypes.c_uint64 * len(BATCH_INFO_KEYS))()
+        _chk(self.ctx.lib.dg_batch_info(self.h, v, len(BATCH_INFO_KEYS)), "batch_info")
+        return dict(zip(BATCH_INFO_KEYS, list(v)))
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.dg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _default_ctx: Context | None = None

@@ -252,6 +252,50 @@ def sphere_field(width=1920, height=1080, n_spheres=500, slices=50, stacks=21, s
     return d
 
 
+def micro_sphere_field(width=3840, height=2160, n_tris=10_000_000, slices=5, stacks=5, seed=1234, tex=4096,
+                       n_lights=4, fov_x=60.0, near_dist=1.0, disc_px=3.6, window=0.4, slab=20.0,
+                       exponent=2) -> SceneDesc:
+    """Stress config: n_tris small triangles as seeded micro UV spheres of
+    2*slices*(stacks-1) triangles each, flattened into one object.
+
+    Every sphere has the same world radius, chosen so its projected disc at the
+    near plane has a radius of about disc_px pixels (about 2 px per triangle);
+    centres lie in a slab of depth slab * radius that starts one radius in front
+    of the near plane, so about 2/slab of the spheres (10% for slab=20) cross
+    it; their screen positions are uniform in a centred window covering
+    window^2 of the screen, which sets the depth complexity (about 8 for the
+    defaults). The statistics actually reached are stored on the description
+    (near_crossing, depth_complexity_est, mean_tri_px_est)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    base_pos, base_nrm, base_uv, base_tri = uv_sphere(1.0, slices, stacks)
+    per = base_tri.shape[0]
+    n_spheres = max(1, n_tris // per)
+    f = (width / 2.0) / math.tan(math.radians(fov_x) / 2.0)  # focal length in pixels
+    r = disc_px * near_dist / f
+    d = rng.uniform(near_dist - r, near_dist - r + slab * r, n_spheres)  # distance along the view axis
+    sx = rng.uniform(-0.5, 0.5, n_spheres) * window * width
+    sy = rng.uniform(-0.5, 0.5, n_spheres) * window * height
+    centres = np.stack([sx * d / f, sy * d / f, -d], -1)
+    nvtx = base_pos.shape[0]
+    pos = (base_pos[None].astype(np.float64) * r + centres[:, None, :]).reshape(-1, 3).astype(np.float32)
+    nrm = np.tile(base_nrm, (n_spheres, 1))
+    uv = np.tile(base_uv, (n_spheres, 1))
+    tri = (base_tri[None].astype(np.int64) + (np.arange(n_spheres) * nvtx)[:, None, None]).reshape(-1, 3)
+    t = value_noise_checker(tex, tex, seed, comps=4)
+    mat = Material((0.1,) * 3, (0.7,) * 3, (0.2,) * 3, 1.0, 0, 0)
+    obj = ObjectDesc(pos, nrm, uv, [MeshDesc(_tris9(tri.astype(np.uint32)), 0)], [mat])
+    lights = np.array([[0.5, 0.8, 0.5], [-0.6, 0.4, -0.2], [0.4, -0.7, -0.3], [-0.5, -0.5, 0.6]],
+                      np.float32)[:n_lights]
+    desc = SceneDesc(width, height, cam_pos=(0.0, 0.0, 0.0), cam_dir=(0.0, 0.0, -1.0), near=-near_dist,
+                     far=-100.0, fov_x=fov_x, lights=lights, exponent=exponent, clear_depth=float("inf"),
+                     textures=[t], objects=[obj], name=f"microspheres{n_spheres}x{per}@{width}x{height}")
+    desc.near_crossing = float(np.mean(np.abs(d - near_dist) < r))
+    disc = math.pi * (disc_px * near_dist / d) ** 2  # projected disc area of each sphere, pixels
+    desc.depth_complexity_est = float(disc.sum() / (window * width * window * height))
+    desc.mean_tri_px_est = float(disc.mean() / (per / 2.0))  # front-facing half of the triangles
+    return desc
+
+
 def near_plane_crossing_fraction(d: SceneDesc, centres: np.ndarray, radii: np.ndarray) -> float:
     """Fraction of sphere instances that intersect the (infinite) near plane."""
     g = np.asarray(d.cam_dir, np.float64)

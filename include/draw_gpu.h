@@ -75,35 +75,40 @@ dg_status dg_ctx_synchronize(dg_ctx* ctx);
 /* Replaces the context's stream (cudaStream_t passed as void*; NULL = own stream). */
 dg_status dg_ctx_set_stream(dg_ctx* ctx, void* stream);
 void* dg_ctx_stream(dg_ctx* ctx);
-/* Per-kernel CUDA-event timing of the last render (ms), up to 6 values: "vertex", "cull",
- * "setup_raster", "queue_raster", "resolve", "shade". Enabled with dg_ctx_set_timing(ctx, 1); the
+/* Per-kernel CUDA-event timing of the last render (ms), up to 5 values: "vertex", "cull",
+ * "setup_raster", "queue_raster", "resolve". Enabled with dg_ctx_set_timing(ctx, 1); the
  * events between kernels also stop their launch overlap, so frames are slower meanwhile. */
 dg_status dg_ctx_set_timing(dg_ctx* ctx, int32_t enable);
 dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
-/* Launch-shape knobs of the raster passes (chosen by draw_gb300.autotune):
+/* Launch-shape knobs of the raster passes (chosen by dg_autotune below):
  * small_max_px: triangles whose clipped bounding box has at most this many
- * pixels are rasterized by the warp that sets them up, the others go to the
- * load-balanced queue pass (0 = all queued, max 4096); setup_blocks_per_sm,
- * queue_blocks_per_sm and cull_blocks_per_sm: grid sizes (caps) of those passes
- * in 256-thread blocks per SM (1..64); record_limit: 0, or at most this many
- * triangle records per render (triangles beyond it are shaded from the mesh
- * again in the resolve pass). Results do not depend on them. */
+ * pixels are rasterized one triangle per lane, the others are cut into 32-pixel
+ * units spread over all warps (0 = all cut into units, max 4096); setup_blocks_per_sm,
+ * queue_blocks_per_sm and cull_blocks_per_sm: grid sizes (caps) of those
+ * passes in 256-thread blocks per SM (1..64); record_limit: 0, or at most this
+ * many triangle records per render (triangles beyond it are shaded from the
+ * mesh again in the resolve pass); tile_rows: height of the resolve pass's
+ * 32-pixel-wide tiles (8, 16 or 32); item_units: 32-pixel units per work item
+ * of the queue pass (1..256). Results do not depend on them. */
 typedef struct {
     uint32_t small_max_px;
     uint32_t setup_blocks_per_sm;
     uint32_t queue_blocks_per_sm;
     uint32_t cull_blocks_per_sm;
     uint32_t record_limit;
+    uint32_t tile_rows;
+    uint32_t item_units;
 } dg_tuning;
 dg_status dg_ctx_set_tuning(dg_ctx* ctx, const dg_tuning* t);
 dg_status dg_ctx_get_tuning(dg_ctx* ctx, dg_tuning* t);
 
-/* Counters of the last render (up to 11): [0] vertices, [1] input triangles, [2] triangles
+/* Counters of the last render (up to 12): [0] vertices, [1] input triangles, [2] triangles
  * queued for the load-balanced raster pass, [3] their 32-pixel work units, [4] covered
- * pixels (written by resolve), [5] large triangles rasterized in place because the queue
- * or the triangle records were full, [6] host-to-device bytes of the job descriptor,
- * [7] kernels launched, [8] triangles that passed the cull pass, [9] triangle records
- * handed out, [10] light/halfway rows handed out to clip vertices. Synchronizes. */
+ * pixels (written by resolve), [5] triangles rasterized in place because the queue, the
+ * small-triangle list or the triangle records were full, [6] host-to-device bytes of the
+ * job descriptor, [7] kernels launched, [8] triangles that passed the cull pass,
+ * [9] triangle records handed out, [10] light/halfway rows handed out to clip vertices,
+ * [11] triangles on the small-triangle list. Synchronizes. */
 dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
 
 /* -------------------------------------------------------------- texture map */
@@ -174,6 +179,33 @@ dg_status dg_scene_render(dg_ctx* ctx, int32_t scene, int32_t canvas);
  * stage (the batched form). Equivalent to n dg_scene_render calls. */
 dg_status dg_render_batch(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n);
 
+/* ---------------------------------------------------- graph-replayed batch
+ * The batched form with its launch sequence captured in a CUDA graph: n
+ * (scene, canvas) frames (scene/canvas ids of ctx) rendered as one job, like
+ * dg_render_batch, but the descriptor upload, the counter reset and the
+ * pipeline kernels are captured once and replayed by each dg_batch_render, so
+ * a replay costs one graph launch on the context stream. Cameras, lights,
+ * exponent, clear depth and canvas offsets may change between replays (the
+ * host rewrites the uploaded descriptors); a change of shape (objects added to
+ * a scene, a canvas resized or destroyed, texture maps added, dg_ctx_set_tuning)
+ * is detected and re-captured at the next dg_batch_render. Each replay renders
+ * exactly what n dg_scene_render calls would. The batch holds its own scratch
+ * memory; kernel errors surface at the context's next synchronizing call. */
+typedef struct dg_batch dg_batch;
+dg_status dg_batch_create(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n, dg_batch** out);
+dg_status dg_batch_render(dg_batch* b);
+/* [0] frames, [1] graph captures, [2] replays, [3] kernels per replay, [4] descriptor bytes per replay. */
+dg_status dg_batch_info(dg_batch* b, uint64_t* out, int32_t n);
+dg_status dg_batch_destroy(dg_batch* b);
+
+/* Launch-shape autotuner: coordinate descent over the dg_tuning knobs on the
+ * caller's frames (two sweeps; each candidate timed with CUDA events over
+ * `reps` renders of the n frames after one warm-up render). Sets the fastest
+ * tuning on ctx and returns it with its time per render in best_ms (either
+ * pointer may be NULL). The knobs do not change what is rendered. */
+dg_status dg_autotune(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n, uint32_t reps,
+                      dg_tuning* best, float* best_ms);
+
 /* ------------------------------------------------------------ render server
  * Serving form of the draw call. The reference renders one frame per call of
  * Scene::render from its application loop (app/mod.rs:196); this server accepts
@@ -223,7 +255,7 @@ dg_status dg_server_destroy(dg_server* s);
  * synchronize the device). It renders one frame of one mesh like
  * dg_scene_render, but all of its scratch memory (vertex records, the
  * visibility buffer, the raster queue, counters, the job descriptor) lives in
- * one statically sized __device__ array of the library (about 5.6 MiB, sized by
+ * one statically sized __device__ array of the library (about 21 MiB, sized by
  * the limits below), which every GPU that loads the library keeps until the
  * process exits. It calls no cudaMalloc, cudaFree or other allocating routine.
  *

@@ -101,7 +101,8 @@ def test_repeat_render_stable(gpu_ctx):
     dict(small_max_px=0), dict(small_max_px=4096),
     dict(setup_blocks_per_sm=1, queue_blocks_per_sm=1, cull_blocks_per_sm=1),
     dict(small_max_px=256, setup_blocks_per_sm=64, queue_blocks_per_sm=64, cull_blocks_per_sm=64),
-    dict(record_limit=1), dict(record_limit=200, small_max_px=0)])
+    dict(record_limit=1), dict(record_limit=200, small_max_px=0),
+    dict(item_units=1, tile_rows=8), dict(item_units=256, tile_rows=16, small_max_px=0)])
 def test_tuning_does_not_change_results(knobs, gpu_ctx, oracle_lib):
     """The raster knobs only move work between the in-warp and queue rasterizers,
     resize grids, or (record_limit) send triangles without a record through the
@@ -118,5 +119,24 @@ def test_tuning_does_not_change_results(knobs, gpu_ctx, oracle_lib):
             st = gpu_ctx.last_stats()
             if knobs.get("record_limit") == 1:
                 assert st["triangle_records"] > 1  # some triangles went without a record
+    finally:
+        gpu_ctx.set_tuning(**before)
+
+
+def test_parity_stress_config(gpu_ctx, oracle_lib):
+    """Stress: 3840x2160, 10M micro-sphere triangles (about 2 px each, depth
+    complexity about 8, 10% of the spheres crossing the near plane), 4096^2
+    texture, 4 lights; with the default launch shapes and with every small
+    triangle on the one-lane-per-triangle path."""
+    desc = S.micro_sphere_field()
+    ref = oracle_render(desc)
+    before = gpu_ctx.get_tuning()
+    try:
+        for knobs in (dict(), dict(small_max_px=64)):
+            gpu_ctx.set_tuning(**knobs)
+            got = gpu_render(desc, gpu_ctx)
+            p = compare(ref, got, desc.clear_depth)
+            print(knobs, describe(p), "near-plane crossing", desc.near_crossing, gpu_ctx.last_stats())
+            assert p.ok and p.n_covered > 500_000, f"{knobs}: {describe(p)}; {first_mismatch(ref, got)}"
     finally:
         gpu_ctx.set_tuning(**before)

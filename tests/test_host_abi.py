@@ -143,13 +143,16 @@ def test_host_only_context_refuses_device_work(lib):
 
 def test_tuning_round_trip_and_validation(lib):
     h = host_ctx(lib)
-    t = (ctypes.c_uint32 * 5)()
+    t = (ctypes.c_uint32 * 7)()
     assert lib.dg_ctx_get_tuning(h, t) == 0
-    assert list(t) == [32, 4, 8, 32, 0]
-    assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 5)(0, 1, 64, 2, 7)) == 0
-    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64, 2, 7]
-    for bad in ((4097, 16, 8, 32, 0), (32, 0, 8, 32, 0), (32, 16, 65, 32, 0), (32, 16, 8, 0, 0)):
-        assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 5)(*bad)) == 1
-    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == [0, 1, 64, 2, 7]
+    assert list(t) == [16, 4, 8, 32, 0, 32, 8]
+    good = (0, 1, 64, 2, 7, 16, 256)
+    assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*good)) == 0
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
+    for bad in ((4097, 16, 8, 32, 0, 8, 8), (32, 0, 8, 32, 0, 8, 8), (32, 16, 65, 32, 0, 8, 8),
+                (32, 16, 8, 0, 0, 8, 8), (32, 16, 8, 8, 0, 0, 8), (32, 16, 8, 8, 0, 12, 8),
+                (32, 16, 8, 8, 0, 64, 8), (32, 16, 8, 8, 0, 8, 0), (32, 16, 8, 8, 0, 8, 257)):
+        assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*bad)) == 1
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
     assert lib.dg_ctx_set_tuning(h, None) == 1
     lib.dg_ctx_destroy(h)

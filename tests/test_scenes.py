@@ -56,3 +56,15 @@ def test_batch_frames_ranges():
         assert 128 <= d.width <= 512 and d.width == d.height
         assert 500 <= d.n_tris <= 6000
         assert d.textures[0].width in (64, 128)
+
+
+def test_micro_sphere_field_statistics():
+    """Stress config shape on a reduced triangle count: the same sphere size,
+    slab and window, so the per-sphere statistics match the full 10M case."""
+    d = S.micro_sphere_field(n_tris=400_000, tex=64)
+    assert d.n_tris == 400_000 and d.objects[0].vertices.shape[0] == 10_000 * 36
+    assert 0.07 < d.near_crossing < 0.13  # about 10% of the spheres cross the near plane
+    assert 1.5 < d.mean_tri_px_est < 2.5  # about 2 px per front-facing triangle
+    assert len(d.lights) == 4
+    full = S.micro_sphere_field.__defaults__
+    assert full[0] == 3840 and full[1] == 2160 and full[2] == 10_000_000 and full[6] == 4096
