@@ -18,8 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
-SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu"]
-HEADERS = ["dg_internal.cuh", "dg_host.h"]
+SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu", "dg_transparent.cu"]
+HEADERS = ["dg_internal.cuh", "dg_host.h", "dg_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",

@@ -271,6 +271,13 @@ dg_status grow(JobSlot& s, T** p, size_t* cap, size_t need) {
     return DG_OK;
 }
 
+void free_object(Object& o) {
+    dfree(o.d_pos); dfree(o.d_nrm); dfree(o.d_uv);
+    dfree(o.d_tri_pos); dfree(o.d_tri_uv); dfree(o.d_tri_nrm); dfree(o.d_mats);
+    for (int b = 0; b < 2; b++)
+        for (int k = 0; k < 3; k++) dfree(o.d_tt[b][k]);
+}
+
 Scene* get_scene(dg_ctx* c, int32_t id) {
     if (!c || id < 0 || (size_t)id >= c->scenes.size()) return nullptr;
     return &c->scenes[id];
@@ -310,7 +317,26 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
     std::vector<FrameTarget> tg;
     dg_status e = resolve_frames(c, scenes, canvases, n, sc, tg);
     if (e) return e;
-    return launch_frames(c, c->main, sc.data(), tg.data(), n);
+    // An object with transparent meshes advances its painter's order once per
+    // render of it; frames that render such an object again start a new job.
+    uint32_t first = 0;
+    std::vector<int32_t> seen;
+    for (uint32_t i = 0; i < n; i++) {
+        bool repeat = false;
+        for (int32_t oid : sc[i]->objects)
+            if (oid >= 0 && (size_t)oid < c->objects.size() && c->objects[oid].nt &&
+                std::find(seen.begin(), seen.end(), oid) != seen.end())
+                repeat = true;
+        if (repeat) {
+            e = launch_frames(c, c->main, sc.data() + first, tg.data() + first, i - first);
+            if (e) return e;
+            first = i;
+            seen.clear();
+        }
+        for (int32_t oid : sc[i]->objects)
+            if (oid >= 0 && (size_t)oid < c->objects.size() && c->objects[oid].nt) seen.push_back(oid);
+    }
+    return launch_frames(c, c->main, sc.data() + first, tg.data() + first, n - first);
 }
 
 }  // namespace dgh
@@ -343,6 +369,12 @@ void slot_free(JobSlot& s) {
     dfree(s.d_queue);
     dfree(s.d_small);
     dfree(s.d_fb);
+    for (int k = 0; k < 2; k++) {
+        dfree(s.d_tkey[k]); dfree(s.d_tval[k]); dfree(s.d_fkey[k]); dfree(s.d_fval[k]);
+    }
+    dfree(s.d_ttrec); dfree(s.d_tbox); dfree(s.d_tmeta); dfree(s.d_talpha); dfree(s.d_tcnt); dfree(s.d_tscan);
+    dfree(s.d_hist);
+    s.tsort_cap = s.tout_cap = s.frag_cap = s.hist_cap = 0;
     dfree(s.d_items);
     dfree(s.d_surv);
     dfree(s.d_rec_of);
@@ -440,14 +472,23 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     frames.assign(n, DgFrameDev{});
     segs.clear();
     uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0, total_px = 0;
+    uint64_t ntt = 0, tmesh_total = 0, max_frame_tt = 0;
     uint32_t stride = 1;
+    B.transparent_objects.clear();
     for (uint32_t i = 0; i < n; i++) {
         Scene& s = *scenes[i];  // frame_setup updates the camera basis, as Scene::render does
         const FrameTarget& tg = targets[i];
         for (int32_t oid : s.objects)
             if (oid < 0 || (size_t)oid >= c->objects.size() || !c->objects[oid].alive) return DG_E_INVALID;
+        // An object with transparent meshes is sorted once per render of it and
+        // keeps the order: a job renders it at most once.
         for (int32_t oid : s.objects)
-            if (!c->objects[oid].transparent.empty()) return DG_E_LIMIT;
+            if (c->objects[oid].nt) {
+                if (std::find(B.transparent_objects.begin(), B.transparent_objects.end(), oid) !=
+                    B.transparent_objects.end())
+                    return DG_E_LIMIT;
+                B.transparent_objects.push_back(oid);
+            }
         DgFrameDev& f = frames[i];
         std::memset(&f, 0, sizeof(f));
         e = frame_setup(s, f.M, f.plane);
@@ -478,6 +519,8 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         f.pix_begin = (uint32_t)total_px;
         total_px += tg.w * tg.h;
         if (total_px >= 0x80000000ull) return DG_E_LIMIT;  // job-wide pixel indices use 31 bits
+        f.tt_begin = (uint32_t)ntt;
+        const uint64_t frame_tt0 = ntt;
         uint64_t seq = 0;
         for (int32_t oid : s.objects) {
             Object& o = c->objects[oid];
@@ -497,15 +540,27 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
             sg.tri_uv = o.d_tri_uv;
             sg.tri_nrm = o.d_tri_nrm;
             sg.mats = o.d_mats;
+            sg.t_begin = (uint32_t)ntt;
+            sg.nt = o.nt;
+            sg.tmesh_base = (uint32_t)tmesh_total;
+            sg.obj_rank = (uint32_t)(segs.size() - f.seg_begin);
+            for (int k = 0; k < 3; k++) {
+                sg.tsrc[k] = o.d_tt[o.tcur][k];
+                sg.tdst[k] = o.d_tt[1 - o.tcur][k];
+            }
             segs.push_back(sg);
             total_tri += o.ntri_opaque;
             total_vtx += o.nv;
             seq += o.ntri_opaque;
+            ntt += o.nt;
+            if (o.nt) tmesh_total += o.tmesh_off.size() - 1;
         }
         if (seq >= (1ull << 30)) return DG_E_LIMIT;
+        max_frame_tt = std::max(max_frame_tt, ntt - frame_tt0);
         f.seg_count = (uint32_t)(segs.size() - f.seg_begin);
     }
     if (total_tri >= 0xFFFFFFFFull || total_vtx >= 0xFFFFFFFFull || total_tiles >= 0x7FFFFFFFull) return DG_E_LIMIT;
+    if (ntt >= (1ull << 29) || tmesh_total >= (1ull << 24)) return DG_E_LIMIT;  // transparent keys and outputs
     if (segs.empty()) {  // keep a valid segment table
         DgSegDev sg;
         std::memset(&sg, 0, sizeof(sg));
@@ -516,8 +571,49 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     e = grow(S, &S.d_vrec, &S.vrec_cap, std::max<uint64_t>(total_vtx, 1));
     if (e) return e;
     const uint64_t vrow_extra = dg_vrow_extra(total_tri);
-    e = grow(S, &S.d_vshade, &S.vshade_cap, (total_vtx + vrow_extra) * stride * 2);
+    // rows: job vertices, clip vertices of opaque triangles, 6 per transparent triangle
+    e = grow(S, &S.d_vshade, &S.vshade_cap, (total_vtx + vrow_extra + 6 * ntt) * stride * 2);
     if (e) return e;
+    const uint64_t fcap = std::min<uint64_t>(2 * total_px + 65536, 0x7FFFFFFFull);
+    if (ntt) {
+        const uint64_t nout = 4 * ntt;
+        if (S.tsort_cap < ntt) {
+            DG_CUDA(cudaStreamSynchronize(S.stream));
+            for (int k = 0; k < 2; k++) {
+                dfree(S.d_tkey[k]);
+                dfree(S.d_tval[k]);
+            }
+            S.tsort_cap = 0;
+            for (int k = 0; k < 2; k++) {
+                if ((e = dalloc(&S.d_tkey[k], ntt)) || (e = dalloc(&S.d_tval[k], ntt))) return e;
+            }
+            S.tsort_cap = ntt;
+        }
+        if (S.tout_cap < nout) {
+            DG_CUDA(cudaStreamSynchronize(S.stream));
+            dfree(S.d_ttrec); dfree(S.d_tbox); dfree(S.d_tmeta); dfree(S.d_talpha); dfree(S.d_tcnt); dfree(S.d_tscan);
+            S.tout_cap = 0;
+            if ((e = dalloc(&S.d_ttrec, nout)) || (e = dalloc(&S.d_tbox, nout)) || (e = dalloc(&S.d_tmeta, nout)) ||
+                (e = dalloc(&S.d_talpha, nout)) || (e = dalloc(&S.d_tcnt, nout)) || (e = dalloc(&S.d_tscan, nout + 1)))
+                return e;
+            S.tout_cap = nout;
+        }
+        if (S.frag_cap < fcap) {
+            DG_CUDA(cudaStreamSynchronize(S.stream));
+            for (int k = 0; k < 2; k++) {
+                dfree(S.d_fkey[k]);
+                dfree(S.d_fval[k]);
+            }
+            S.frag_cap = 0;
+            for (int k = 0; k < 2; k++) {
+                if ((e = dalloc(&S.d_fkey[k], fcap)) || (e = dalloc(&S.d_fval[k], fcap))) return e;
+            }
+            S.frag_cap = fcap;
+        }
+        const uint64_t tiles = (std::max(ntt, fcap) + DG_SORT_TILE - 1) / DG_SORT_TILE;
+        e = grow(S, &S.d_hist, &S.hist_cap, 256 * tiles);
+        if (e) return e;
+    }
     e = grow(S, &S.d_surv, &S.surv_cap, std::max<uint64_t>(total_tri, 1));
     if (e) return e;
     e = grow(S, &S.d_rec_of, &S.rec_of_cap, std::max<uint64_t>(total_tri, 1));
@@ -556,7 +652,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.shade_stride = stride;
     job.vrec = S.d_vrec;
     job.vshade = S.d_vshade;
-    job.vrow_extra = (uint32_t)std::min<uint64_t>(S.vshade_cap / (2ull * stride) - total_vtx, 0xFFFFFFF0ull);
+    job.vrow_extra = (uint32_t)vrow_extra;
     job.vmark = S.d_vmark;
     job.surv = S.d_surv;
     job.rec_of = S.d_rec_of;
@@ -579,6 +675,47 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.ntex = (uint32_t)c->tex.size();
     job.err = S.d_err;
     B.launches = (total_vtx ? 1 : 0) + (total_tri ? 3 : 0) + (total_tiles ? 2 : 0);
+    B.cfg.tplan = DgTransparentPlan{};
+    if (ntt) {
+        job.ntt = (uint32_t)ntt;
+        job.fcap = (uint32_t)fcap;
+        for (int k = 0; k < 2; k++) {
+            job.tkey[k] = S.d_tkey[k];
+            job.tval[k] = S.d_tval[k];
+            job.fkey[k] = S.d_fkey[k];
+            job.fval[k] = S.d_fval[k];
+        }
+        job.ttrec = S.d_ttrec;
+        job.tbox = S.d_tbox;
+        job.tmeta = S.d_tmeta;
+        job.talpha = S.d_talpha;
+        job.tcnt = S.d_tcnt;
+        job.tscan = S.d_tscan;
+        job.sort_hist = S.d_hist;
+        job.hist_tiles = (uint32_t)(S.hist_cap / 256);
+        // radix digits: the painter's keys are (mesh << 32 | distance key), the
+        // fragment keys (pixel << 32 | frame-local transparent key)
+        auto bits = [](uint64_t v) {
+            uint32_t b = 0;
+            while (v) {
+                b++;
+                v >>= 1;
+            }
+            return b;
+        };
+        DgTransparentPlan& p = B.cfg.tplan;
+        auto add = [](uint32_t* sh, uint32_t& np, uint32_t lo, uint32_t nbits) {
+            for (uint32_t b = 0; b < nbits; b += 8) sh[np++] = lo + b;
+        };
+        add(p.tsort_shift, p.n_tsort, 0, 32);
+        add(p.tsort_shift, p.n_tsort, 32, bits(tmesh_total - 1));
+        if (p.n_tsort & 1u) p.tsort_shift[p.n_tsort++] = 56;  // even pass count: the result lands in buffer 0
+        add(p.fsort_shift, p.n_fsort, 0, bits(4 * max_frame_tt - 1));
+        add(p.fsort_shift, p.n_fsort, 32, bits(total_px - 1));
+        if (p.n_fsort & 1u) p.fsort_shift[p.n_fsort++] = 56;
+        p.blocks = (unsigned)c->nsm * 8u;
+        B.launches += 3 * (p.n_tsort + p.n_fsort) + 6;
+    }
     B.cfg.cull_blocks = (unsigned)c->nsm * S.cull_blocks_per_sm;
     B.cfg.setup_blocks = (unsigned)c->nsm * S.setup_blocks_per_sm;
     B.cfg.queue_blocks = (unsigned)c->nsm * S.queue_blocks_per_sm;
@@ -594,6 +731,10 @@ dg_status enqueue_job(JobBuild& B, JobSlot& S, void* d_stage, cudaStream_t strea
     DG_CUDA(cudaMemsetAsync(S.d_counters, 0, DG_NCOUNTERS * sizeof(unsigned long long), stream));
     DG_CUDA(dg_launch_job(B.job, B.cfg, stream, timing ? S.ev : nullptr));
     return DG_OK;
+}
+
+void advance_transparent(dg_ctx* c, const JobBuild& b) {
+    for (int32_t oid : b.transparent_objects) c->objects[oid].tcur ^= 1;
 }
 
 dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n) {
@@ -627,6 +768,7 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     S.last_launches = B.launches;
     e = enqueue_job(B, S, S.d_stage[k], S.stream, S.timing);
     if (e) return e;
+    advance_transparent(c, B);
     if (S.timing) S.ev_valid = true;
     return DG_OK;
 }
@@ -707,10 +849,7 @@ dg_status dg_ctx_destroy(dg_ctx* c) {
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
     for (auto& t : c->tex) dfree(t.d_words);
-    for (auto& o : c->objects) {
-        dfree(o.d_pos); dfree(o.d_nrm); dfree(o.d_uv);
-        dfree(o.d_tri_pos); dfree(o.d_tri_uv); dfree(o.d_tri_nrm); dfree(o.d_mats);
-    }
+    for (auto& o : c->objects) free_object(o);
     for (auto& v : c->canvases) {
         dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
     }
@@ -853,6 +992,8 @@ dg_status dg_object_create(dg_ctx* c, const float* vertices, uint64_t nv, const 
     }
     Object o;
     std::vector<uint4> tpos, tuv, tnrm;
+    std::vector<uint4> xpos, xuv, xnrm;  // transparent meshes
+    o.tmesh_off.push_back(0u);
     uint64_t total = 0;
     for (uint64_t m = 0; m < nmesh; m++) {
         if (meshes[m].ntri && !meshes[m].tris) return DG_E_INVALID;
@@ -870,8 +1011,14 @@ dg_status dg_object_create(dg_ctx* c, const float* vertices, uint64_t nv, const 
         const dg_mesh_desc& md = meshes[m];
         bool transparent = mats[md.texture_idx].alpha < 1.0f;
         if (transparent) {
-            o.transparent.emplace_back(md.tris, md.tris + 9 * md.ntri);
-            o.transparent_mat.push_back(md.texture_idx);
+            const uint32_t mesh = (uint32_t)(o.tmesh_off.size() - 1);
+            for (uint64_t t = 0; t < md.ntri; t++) {
+                const uint32_t* q = md.tris + 9 * t;
+                xpos.push_back(make_uint4(q[0], q[1], q[2], (uint32_t)md.texture_idx));
+                xuv.push_back(make_uint4(q[3], q[4], q[5], mesh));
+                xnrm.push_back(make_uint4(q[6], q[7], q[8], 0u));
+            }
+            o.tmesh_off.push_back((uint32_t)xpos.size());
             continue;
         }
         for (uint64_t t = 0; t < md.ntri; t++) {
@@ -886,8 +1033,8 @@ dg_status dg_object_create(dg_ctx* c, const float* vertices, uint64_t nv, const 
     for (uint64_t i = 0; i < nv; i++) p4[i] = make_float4(vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2], 1.0f);
     for (uint64_t i = 0; i < nn; i++) n4[i] = make_float4(normals[3 * i], normals[3 * i + 1], normals[3 * i + 2], 0.0f);
     for (uint64_t i = 0; i < nuv; i++) u2[i] = make_float2(uvs[3 * i], uvs[3 * i + 1]);
-    o.h_pos.assign(vertices, vertices + 3 * nv);
     o.nv = (uint32_t)nv;
+    o.nt = (uint32_t)xpos.size();
     o.nn = (uint32_t)nn;
     o.nuv = (uint32_t)nuv;
     o.ntri_opaque = (uint32_t)tpos.size();
@@ -900,9 +1047,11 @@ dg_status dg_object_create(dg_ctx* c, const float* vertices, uint64_t nv, const 
         return DG_OK;
     };
     if ((e = up(&o.d_pos, p4)) || (e = up(&o.d_nrm, n4)) || (e = up(&o.d_uv, u2)) || (e = up(&o.d_tri_pos, tpos)) ||
-        (e = up(&o.d_tri_uv, tuv)) || (e = up(&o.d_tri_nrm, tnrm)) || (e = up(&o.d_mats, dm))) {
-        dfree(o.d_pos); dfree(o.d_nrm); dfree(o.d_uv);
-        dfree(o.d_tri_pos); dfree(o.d_tri_uv); dfree(o.d_tri_nrm); dfree(o.d_mats);
+        (e = up(&o.d_tri_uv, tuv)) || (e = up(&o.d_tri_nrm, tnrm)) || (e = up(&o.d_mats, dm)) ||
+        (e = up(&o.d_tt[0][0], xpos)) || (e = up(&o.d_tt[0][1], xuv)) || (e = up(&o.d_tt[0][2], xnrm)) ||
+        (e = dalloc(&o.d_tt[1][0], xpos.size())) || (e = dalloc(&o.d_tt[1][1], xpos.size())) ||
+        (e = dalloc(&o.d_tt[1][2], xpos.size()))) {
+        free_object(o);
         return e;
     }
     o.alive = true;
@@ -919,8 +1068,7 @@ dg_status dg_object_destroy(dg_ctx* c, int32_t id) {
             if (x == id) return DG_E_INVALID;  // still referenced by a scene
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    dfree(o->d_pos); dfree(o->d_nrm); dfree(o->d_uv);
-    dfree(o->d_tri_pos); dfree(o->d_tri_uv); dfree(o->d_tri_nrm); dfree(o->d_mats);
+    free_object(*o);
     o->alive = false;
     return DG_OK;
 }
@@ -1000,12 +1148,23 @@ dg_status dg_scene_frame_setup(dg_ctx* c, int32_t scene, float M[16], float plan
 dg_status dg_object_transparent_tris(dg_ctx* c, int32_t object, uint32_t mesh, uint32_t* out, uint64_t cap,
                                      uint64_t* out_ntri) {
     Object* o = get_object(c, object);
-    if (!o || mesh >= o->transparent.size()) return DG_E_INVALID;
-    const auto& t = o->transparent[mesh];
-    if (out_ntri) *out_ntri = t.size() / 9;
-    if (out) {
-        if (cap < t.size()) return DG_E_INVALID;
-        std::memcpy(out, t.data(), t.size() * 4);
+    if (!o || (size_t)mesh + 1 >= o->tmesh_off.size()) return DG_E_INVALID;
+    const uint32_t b = o->tmesh_off[mesh], n = o->tmesh_off[mesh + 1] - b;
+    if (out_ntri) *out_ntri = n;
+    if (!out || n == 0) return DG_OK;
+    if (cap < 9ull * n) return DG_E_INVALID;
+    dg_status e = set_device(c);
+    if (e) return e;
+    DG_CUDA(cudaStreamSynchronize(c->main.stream));
+    std::vector<uint4> a[3];
+    for (int k = 0; k < 3; k++) {
+        a[k].resize(n);
+        DG_CUDA(cudaMemcpy(a[k].data(), o->d_tt[o->tcur][k] + b, n * sizeof(uint4), cudaMemcpyDeviceToHost));
+    }
+    for (uint32_t t = 0; t < n; t++) {  // (position, uv, normal) index triples, as the mesh was given
+        const uint4 p = a[0][t], u = a[1][t], q = a[2][t];
+        const uint32_t row[9] = {p.x, p.y, p.z, u.x, u.y, u.z, q.x, q.y, q.z};
+        std::memcpy(out + 9ull * t, row, sizeof(row));
     }
     return DG_OK;
 }

@@ -239,6 +239,7 @@ dg_status dg_batch_render(dg_batch* b) {
     std::memcpy((uint8_t*)b->h_stage[k] + B.fbytes, B.segs.data(), B.sbytes);
     DG_CUDA(cudaGraphLaunch(b->exec[k], c->main.stream));
     DG_CUDA(cudaEventRecord(b->done[k], c->main.stream));
+    advance_transparent(c, B);
     b->replays++;
     return DG_OK;
 }

@@ -74,9 +74,16 @@ struct Object {
     uint4* d_tri_nrm = nullptr;
     DgMatDev* d_mats = nullptr;
     uint32_t nv = 0, nn = 0, nuv = 0, ntri_opaque = 0, nmats = 0;
-    std::vector<float> h_pos;                        // for the transparent pass sort
-    std::vector<std::vector<uint32_t>> transparent;  // 9 indices per triangle, current order
-    std::vector<int32_t> transparent_mat;
+    // Transparent meshes (object.rs:45-53: material alpha < 1), concatenated in
+    // mesh order: mesh m holds triangles [tmesh_off[m], tmesh_off[m + 1]) as
+    // (position indices, material), (uv indices, m), (normal indices). The
+    // painter's sort of every frame reorders each mesh and the order persists
+    // (scene/mod.rs:1100-1115): d_tt[tcur] holds the current order, and a
+    // render writes the next one into d_tt[1 - tcur].
+    uint4* d_tt[2][3] = {};
+    int tcur = 0;
+    uint32_t nt = 0;
+    std::vector<uint32_t> tmesh_off;
 };
 
 struct Canvas {
@@ -115,6 +122,22 @@ struct JobSlot {
     size_t small_cap = 0;
     uint32_t* d_fb = nullptr;  // resolve fallback tile list
     size_t fb_cap = 0;
+    // transparent pass scratch (DgJobDev)
+    uint64_t* d_tkey[2] = {};
+    uint32_t* d_tval[2] = {};
+    size_t tsort_cap = 0;
+    DgTriRec* d_ttrec = nullptr;
+    uint4* d_tbox = nullptr;
+    uint2* d_tmeta = nullptr;
+    float* d_talpha = nullptr;
+    uint32_t* d_tcnt = nullptr;
+    unsigned long long* d_tscan = nullptr;
+    size_t tout_cap = 0;  // clip outputs the arrays above hold (tscan: one more)
+    uint64_t* d_fkey[2] = {};
+    uint32_t* d_fval[2] = {};
+    size_t frag_cap = 0;
+    uint32_t* d_hist = nullptr;
+    size_t hist_cap = 0;  // entries
     uint2* d_items = nullptr;  // raster work items
     size_t queue_cap = 0;
     size_t items_cap = 0;
@@ -187,6 +210,7 @@ struct JobBuild {
     DgJobDev job{};
     DgLaunchCfg cfg{};
     uint64_t total_vtx = 0, total_tri = 0, launches = 0;
+    std::vector<int32_t> transparent_objects;  // objects whose transparent order the job advances
 };
 // Host frame setup of every frame (camera basis, matrix, view planes) and the
 // scratch sizing of slot s (grows its buffers; synchronizes s only when one grows).
@@ -201,5 +225,8 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
 // Enqueues the counter reset and the kernels of a built job whose descriptors
 // are (or will be, in stream order) at d_stage on the device.
 dg_status enqueue_job(JobBuild& b, JobSlot& s, void* d_stage, cudaStream_t stream, bool timing);
+// After a job is enqueued: the painter's order it wrote becomes each
+// transparent object's current order.
+void advance_transparent(dg_ctx* c, const JobBuild& b);
 
 }  // namespace dgh

@@ -72,7 +72,8 @@ struct alignas(16) DgFrameDev {
     uint32_t seg_begin, seg_count;  // this frame's segments (ascending seq_base)
     uint32_t tile_begin, tiles_x;   // this frame's resolve tiles
     uint32_t pix_begin;             // job-wide index of this frame's first pixel
-    uint32_t pad[3];
+    uint32_t tt_begin;              // job-wide index of this frame's first transparent triangle
+    uint32_t pad[2];
 };
 static_assert(sizeof(DgTexDev) == 48 && sizeof(DgMatDev) == 48, "descriptor sizes");
 inline uint32_t dg_tex_small(uint64_t len, uint64_t w, uint64_t h) {
@@ -100,6 +101,16 @@ struct DgSegDev {
     const uint4* tri_uv;
     const uint4* tri_nrm;
     const DgMatDev* mats;
+    // The object's transparent triangles (the transparent pass): position
+    // indices + material, uv indices + mesh within the object (w), normal
+    // indices, in their current order (src) and after this frame's painter's
+    // sort (dst), which becomes the current order of the next frame.
+    uint32_t t_begin;     // job-wide index of the first transparent triangle
+    uint32_t nt;          // transparent triangles of the object
+    uint32_t tmesh_base;  // job-wide index of the object's first transparent mesh
+    uint32_t obj_rank;    // the object's position within its frame
+    const uint4* tsrc[3];
+    uint4* tdst[3];
 };
 
 // Edge constants of one triangle: f_k(x, y) = ((A[k]*x + B[k]*y) + C[k]) - D[k]
@@ -157,7 +168,8 @@ struct alignas(16) DgQueueRec {
 #define DG_CNT_SMALL 7    // entries of the small-triangle list
 #define DG_CNT_TRECX 8    // records handed out after the first total_tri (multi-output clips)
 #define DG_CNT_FBTILES 9  // entries of the fallback tile list
-#define DG_NCOUNTERS 10
+#define DG_CNT_TFRAG 10   // transparent fragments emitted
+#define DG_NCOUNTERS 12
 
 struct DgJobDev {
     const DgFrameDev* frames;
@@ -188,6 +200,30 @@ struct DgJobDev {
     const DgTexDev* tex;
     uint32_t ntex;          // entries of tex
     uint32_t* err;
+    // Transparent pass (all null/zero when the job has no transparent triangle).
+    uint32_t ntt;           // transparent triangles of the job
+    uint32_t fcap;          // capacity of the fragment buffers
+    uint64_t* tkey[2];      // painter's sort: keys and source slots, [ntt] each
+    uint32_t* tval[2];
+    DgTriRec* ttrec;        // [4 ntt] records of clip outputs, 4 j + o for sorted slot j
+    uint4* tbox;            // [4 ntt] (xlo, ylo, width, frame) of each output's bounding box
+    uint2* tmeta;           // [4 ntt] (object rank within the frame, frame-local transparent key)
+    float* talpha;          // [4 ntt] material alpha
+    uint32_t* tcnt;         // [4 ntt] bounding-box pixels of each output, 0 for none
+    unsigned long long* tscan;  // [4 ntt + 1] exclusive prefix sums of tcnt
+    uint64_t* fkey[2];      // fragments: (job-wide pixel << 32 | transparent key), output record
+    uint32_t* fval[2];
+    uint32_t* sort_hist;    // radix sort histograms, 256 per tile of DG_SORT_TILE keys
+    uint32_t hist_tiles;    // tiles sort_hist has room for
+};
+
+// Launch plan of the transparent pass: the digit shifts of its two radix
+// sorts (painter's sort keys, fragment keys) and the grid of its grid-stride
+// kernels.
+struct DgTransparentPlan {
+    uint32_t tsort_shift[8], n_tsort;  // painter's sort digits
+    uint32_t fsort_shift[8], n_fsort;  // fragment sort digits
+    unsigned blocks;                   // grid of the grid-stride kernels
 };
 
 // Host-side launchers (dg_kernels.cu).
@@ -196,14 +232,21 @@ struct DgLaunchCfg {
     unsigned setup_blocks;
     unsigned queue_blocks;
     unsigned fallback_blocks;
+    DgTransparentPlan tplan;
 };
 #define DG_SETUP_BLOCKS_PER_SM 4u
 #define DG_QUEUE_BLOCKS_PER_SM 8u
 #define DG_CULL_BLOCKS_PER_SM 32u
-#define DG_NKERNELS 5  // vertex, cull, setup_raster, queue_raster, resolve
+#define DG_NKERNELS 5  // vertex, cull, setup_raster, queue_raster, resolve (+ the transparent pass)
+#define DG_SORT_TILE 4096u  // keys per radix-sort tile (256 threads x 16)
 // Launches the whole pipeline of one job on stream s. ev, if not null, holds
 // DG_NKERNELS + 1 events recorded around the kernels (per-kernel timing).
 cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev);
+// The transparent pass (dg_transparent.cu), in three parts launched by
+// dg_launch_job: part 0 after the opaque setup (painter's sort, gather,
+// transparent setup), part 1 after the opaque raster (fragment emission and
+// sort), part 2 after the opaque resolve (the ordered blend).
+cudaError_t dg_launch_transparent(int part, const DgJobDev& job, const DgTransparentPlan& plan, cudaStream_t s);
 // Scratch rows and records sized for a job of T triangles (shared sizing rule).
 constexpr uint64_t dg_trec_cap(uint64_t T) { return T + T / 8u + 4096u; }
 constexpr uint64_t dg_items_cap(uint64_t queue_cap) { return 2u * queue_cap + 65536u; }

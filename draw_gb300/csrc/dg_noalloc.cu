@@ -237,7 +237,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     NA_CUDA(cudaMemsetAsync(base + kOffWhite, 0xFF, 8, s));
     NA_CUDA(dg_launch_vis_reset(reinterpret_cast<uint64_t*>(base + kOffVis), npx, s));
 
-    DgLaunchCfg cfg;
+    DgLaunchCfg cfg{};
     cfg.cull_blocks = (unsigned)nsm * DG_CULL_BLOCKS_PER_SM;
     cfg.setup_blocks = (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM;
     cfg.queue_blocks = (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM;

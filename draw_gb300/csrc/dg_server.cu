@@ -304,7 +304,7 @@ dg_status dg_server_submit(dg_server* s, const dg_request* q, uint64_t* ticket) 
     if (!s || !q || !ticket) return DG_E_INVALID;
     dg_ctx* c = s->ctx;
     if (q->object < 0 || (size_t)q->object >= c->objects.size() || !c->objects[q->object].alive) return DG_E_INVALID;
-    if (!c->objects[q->object].transparent.empty()) return DG_E_LIMIT;
+    if (c->objects[q->object].nt > 0) return DG_E_LIMIT;  // requests render opaque meshes only
     if (q->width == 0 || q->height == 0 || q->width > 65535 || q->height > 65535) return DG_E_INVALID;
     if (q->nlights == 0 || q->nlights > DG_MAX_LIGHTS) return DG_E_INVALID;
     auto r = std::make_unique<Request>();

@@ -384,6 +384,18 @@ class Object:
         self.meshes = meshes
         self.textures = textures
 
+    def transparent_triangles(self, mesh: int) -> np.ndarray:
+        """The current (painter's sort) order of transparent mesh `mesh` as (T, 9)
+        indices; Scene::render re-sorts it every frame and keeps it (scene/mod.rs:1100-1115)."""
+        n = ctypes.c_uint64()
+        _chk(self.ctx.lib.dg_object_transparent_tris(self.ctx.h, self.id, mesh, None, 0, ctypes.byref(n)),
+             "transparent_tris")
+        out = np.zeros((n.value, 9), np.uint32)
+        if n.value:
+            _chk(self.ctx.lib.dg_object_transparent_tris(self.ctx.h, self.id, mesh, _ptr(out), out.size,
+                                                         ctypes.byref(n)), "transparent_tris")
+        return out
+
     def mesh_info_list(self) -> list:  # object.rs:456-476 (opaque meshes first, then transparent)
         op = [m for m in self.meshes if self.textures[m.texture_idx].alpha >= 1.0 or
               np.isnan(self.textures[m.texture_idx].alpha)]

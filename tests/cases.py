@@ -164,3 +164,79 @@ PARITY_CASES = {
     "torus_rgb": lambda: S.torus_scene(width=300, height=200, nu=30, nv=12, tex=100, comps=3),
     "sphere_field_small": small_sphere_field,
 }
+
+
+# ------------------------------------------------------------ transparency
+def _quad(x0, y0, x1, y1, z):
+    """Two triangles facing +z (the flat_scene camera), corners counter-clockwise."""
+    return [[x0, y0, z], [x1, y0, z], [x1, y1, z], [x0, y1, z]], [[0, 1, 2], [0, 2, 3]]
+
+
+def _quads(spec):
+    pos, tris = [], []
+    for q in spec:
+        p, t = _quad(*q)
+        tris += [[i + len(pos) for i in tri] for tri in t]
+        pos += p
+    return pos, tris
+
+
+def _tmat(alpha, map_idx=0, ka=0.3, kd=0.6, ks=0.25):
+    return S.Material((ka,) * 3, (kd, kd * 0.8, kd * 0.6), (ks,) * 3, alpha, map_idx, map_idx)
+
+
+def transparent_scene() -> S.SceneDesc:
+    """Object 0: an opaque quad with two transparent meshes (alpha 0.5 and
+    0.25) in front of and behind it; object 1: an opaque quad between object 0's
+    transparent layers (drawn after them, it overwrites their blend where it is
+    nearer than the opaque quad); object 2: transparent only, in front of
+    everything, with a default (white) map."""
+    tex = [S.value_noise_checker(64, 64, 31), S.value_noise_checker(32, 48, 32, comps=3)]
+    p0, t0 = _quads([(-3, -2, 3, 2, 0.0), (-2.5, -1.5, 1.0, 1.5, 1.0), (-1.0, -1.8, 2.5, 0.5, 2.0),
+                     (0.5, -1.0, 3.5, 2.5, 3.0), (-3.5, -2.5, -0.5, 0.5, -1.0), (-2.0, 0.5, 2.8, 2.2, 4.0)])
+    o0 = _obj(p0, t0, [_mat(0), _tmat(0.5, 0), _tmat(0.25, 1)], mesh_split=[(2, 0), (6, 1), (4, 2)])
+    p1, t1 = _quads([(-1.5, -1.2, 0.8, 0.9, 2.5)])
+    o1 = _obj(p1, t1, [_mat(1, ka=0.5, kd=0.4)])
+    p2, t2 = _quads([(-2.2, -0.6, 0.2, 1.9, 5.0), (-0.5, -2.4, 1.5, -0.2, 5.5)])
+    o2 = _obj(p2, t2, [S.Material((0.2,) * 3, (0.9, 0.3, 0.2), (0.4,) * 3, 0.6, -1, -1)])
+    return flat_scene([o0, o1, o2], width=96, height=72, textures=tex)
+
+
+def transparent_clip_scene() -> S.SceneDesc:
+    """Transparent triangles crossing the near plane (both clip outputs), over an opaque torus."""
+    pos, nrm, uv, tri = S.torus(1.0, 0.4, 24, 10)
+    op = S.ObjectDesc(pos, nrm, uv, [S.MeshDesc(S._tris9(tri), 0)], [_mat(0)])
+    rng = np.random.Generator(np.random.PCG64(41))
+    tpos = rng.uniform(-2.0, 2.0, (60, 3)).astype(np.float32)
+    tpos[:, 2] = rng.uniform(1.0, 3.4, 60).astype(np.float32)  # the camera sits at z = 3, near plane at 2.5
+    tt = rng.integers(0, 60, (40, 3)).astype(np.uint32)
+    tr = _obj(tpos, tt, [_tmat(0.4, 0), _tmat(0.7, 0)], mesh_split=[(25, 0), (15, 1)])
+    return S.SceneDesc(120, 90, cam_pos=(0.0, 0.0, 3.0), cam_dir=(0.0, 0.0, -1.0), near=-0.5, far=-20.0,
+                       fov_x=80.0, lights=np.array([[2.0, 3.0, 4.0], [-3.0, 1.0, 2.0]], np.float32), exponent=3,
+                       textures=[S.value_noise_checker(64, 64, 43)], objects=[op, tr])
+
+
+def transparent_ties_scene() -> S.SceneDesc:
+    """A transparent mesh whose triangles come in groups of four at exactly equal
+    centre distances from any camera on the z axis (rotations by 90 degrees about
+    it), so the stable painter's sort must keep the previous frame's order among
+    them; plus an opaque backdrop."""
+    base = np.array([[1.0, 0.0, 0.0], [2.0, 0.5, 0.0], [1.5, 1.5, 0.0]], np.float32)
+    pos, tris = [], []
+    for layer, z in enumerate((1.5, 0.5, 1.0)):  # mesh 0: the nearer layer first, so the sort moves it
+        for r in range(4):
+            c, s = [(1, 0), (0, 1), (-1, 0), (0, -1)][r]
+            for v in base:
+                pos.append([c * v[0] - s * v[1], s * v[0] + c * v[1], z])
+            tris.append([len(pos) - 3, len(pos) - 2, len(pos) - 1])
+    tr = _obj(pos, tris, [_tmat(0.5, 0), _tmat(0.3, 0)], mesh_split=[(8, 0), (4, 1)])
+    bp, bt = _quads([(-3, -3, 3, 3, -0.5)])
+    bg = _obj(bp, bt, [_mat(0)])
+    return flat_scene([bg, tr], width=80, height=80, textures=[S.value_noise_checker(32, 32, 51)])
+
+
+TRANSPARENT_CASES = {
+    "transparent": transparent_scene,
+    "transparent_clip": transparent_clip_scene,
+    "transparent_ties": transparent_ties_scene,
+}
