@@ -18,7 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
-SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu", "dg_transparent.cu"]
+SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu", "dg_transparent.cu",
+           "dg_loader.cpp"]
 HEADERS = ["dg_internal.cuh", "dg_host.h", "dg_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -52,7 +53,7 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
     objs = []
     cmds = []
     for s in SOURCES:
-        obj = os.path.join(LIBDIR, s.replace(".cu", f".{tag}.o"))
+        obj = os.path.join(LIBDIR, os.path.splitext(s)[0] + f".{tag}.o")
         objs.append(obj)
         cmds.append([nvcc(), *ARCH, *NVCC_FLAGS, *(extra or []), "-c", os.path.join(CSRC, s), "-o", obj])
     with cf.ThreadPoolExecutor(len(cmds)) as ex:

@@ -363,7 +363,7 @@ dg_status slot_init(dg_ctx* c, JobSlot& s, cudaStream_t stream) {
 
 void slot_free(JobSlot& s) {
     if (s.stream) cudaStreamSynchronize(s.stream);
-    dfree(s.d_vrec);
+    dfree(s.d_vmask);
     dfree(s.d_vshade);
     dfree(s.d_vmark);
     dfree(s.d_queue);
@@ -449,7 +449,7 @@ uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L
         return (cap >= need && p) ? cap : std::max(need, cap * 3 / 2);
     };
     if (L == 0) L = 1;
-    const size_t vrec = cap_after(s.vrec_cap, s.d_vrec, std::max<uint64_t>(V, 1));
+    const size_t vmask = cap_after(s.vmask_cap, s.d_vmask, std::max<uint64_t>(V, 1));
     const size_t vshade = cap_after(s.vshade_cap, s.d_vshade, (V + dg_vrow_extra(T)) * L * 2);
     const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>((V + 31) / 32, 1));
     const size_t q = cap_after(s.queue_cap, s.d_queue, queue_records(T));
@@ -459,7 +459,7 @@ uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L
     const size_t sv = cap_after(s.surv_cap, s.d_surv, std::max<uint64_t>(T, 1));
     const size_t ro = cap_after(s.rec_of_cap, s.d_rec_of, std::max<uint64_t>(T, 1));
     const size_t tr = cap_after(s.trec_cap, s.d_trec, trec_records(T));
-    return vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + (q + sm) * sizeof(DgQueueRec) +
+    return vmask * sizeof(uint16_t) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + (q + sm) * sizeof(DgQueueRec) +
            qb * sizeof(uint2) + (sv + ro + fb) * sizeof(uint32_t) + tr * sizeof(DgTriRec);
 }
 
@@ -568,7 +568,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     }
     e = sync_tex_table(c, S.stream);
     if (e) return e;
-    e = grow(S, &S.d_vrec, &S.vrec_cap, std::max<uint64_t>(total_vtx, 1));
+    e = grow(S, &S.d_vmask, &S.vmask_cap, std::max<uint64_t>(total_vtx, 1));
     if (e) return e;
     const uint64_t vrow_extra = dg_vrow_extra(total_tri);
     // rows: job vertices, clip vertices of opaque triangles, 6 per transparent triangle
@@ -650,7 +650,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.total_tri = (uint32_t)total_tri;
     job.total_tiles = (uint32_t)total_tiles;
     job.shade_stride = stride;
-    job.vrec = S.d_vrec;
+    job.vmask = S.d_vmask;
     job.vshade = S.d_vshade;
     job.vrow_extra = (uint32_t)vrow_extra;
     job.vmark = S.d_vmark;
@@ -855,6 +855,14 @@ dg_status dg_ctx_destroy(dg_ctx* c) {
     }
     dfree(c->d_tex);
     slot_free(c->main);
+    {
+        OverlaySlot& O = c->overlay;
+        dfree(O.d_rec); dfree(O.d_box); dfree(O.d_scan); dfree(O.d_hist); dfree(O.d_cnt); dfree(O.d_rgba);
+        for (int k = 0; k < 2; k++) {
+            dfree(O.d_fkey[k]);
+            dfree(O.d_fval[k]);
+        }
+    }
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return DG_OK;
@@ -1296,6 +1304,212 @@ dg_status dg_canvas_device_ptrs(dg_ctx* c, int32_t id, void** bgra, void** depth
     if (bgra) *bgra = v->d_colour;
     if (depth) *depth = v->d_depth;
     return DG_OK;
+}
+
+namespace {
+
+// Rust `as usize` from f32 (saturating, NaN -> 0), on the host.
+uint64_t h_as_usize(float f) {
+    if (!(f > 0.0f)) return 0ull;
+    if (f >= 18446744073709551616.0f) return ~0ull;
+    return (uint64_t)f;
+}
+
+// Rectangle (canvas.rs:293-351) in usize arithmetic.
+struct HRect {
+    uint64_t x, y, w, h;
+    static HRect from_coords(uint64_t x0, uint64_t y0, uint64_t x1, uint64_t y1) {
+        const uint64_t xa = std::min(x0, x1), ya = std::min(y0, y1), xb = std::max(x0, x1), yb = std::max(y0, y1);
+        return HRect{xa, ya, xb - xa, yb - ya};
+    }
+    static HRect clip(const HRect& a, const HRect& b) {
+        uint64_t x0 = std::max(a.x, b.x), y0 = std::max(a.y, b.y);
+        uint64_t x1 = std::min(a.x + a.w, b.x + b.w), y1 = std::min(a.y + a.h, b.y + b.h);
+        if (x0 > x1) x0 = x1 = 0;
+        if (y0 > y1) y0 = y1 = 0;
+        return from_coords(x0, y0, x1, y1);
+    }
+};
+
+// The edge set of dg_device.cuh make_edges, on the host (the same f32
+// operations; this file is compiled without contraction), as the 16 words of
+// a triangle record: A[3], B[3], C[3], D[3], den[3], tie bits.
+void host_edges(float ax, float ay, float bx, float by, float cx, float cy, float w[16]) {
+    const float px[3] = {bx, cx, ax}, py[3] = {by, cy, ay};
+    const float qx[3] = {cx, ax, bx}, qy[3] = {cy, ay, by};
+    const float vx[3] = {ax, bx, cx}, vy[3] = {ay, by, cy};
+    float A[3], B[3], C[3], D[3], den[3];
+    uint32_t tie = 0;
+    for (int k = 0; k < 3; k++) {
+        A[k] = py[k] - qy[k];
+        B[k] = qx[k] - px[k];
+        C[k] = px[k] * qy[k];
+        D[k] = qx[k] * py[k];
+    }
+    auto eval = [&](int k, float x, float y) { return ((A[k] * x + B[k] * y) + C[k]) - D[k]; };
+    for (int k = 0; k < 3; k++) {
+        den[k] = eval(k, vx[k], vy[k]);
+        if (den[k] * eval(k, -1.0f, -1.0f) > 0.0f) tie |= 1u << k;
+    }
+    bool fast = true;
+    for (int k = 0; k < 3; k++) {
+        if (std::signbit(den[k])) {
+            A[k] = -A[k];
+            B[k] = -B[k];
+            C[k] = -C[k];
+            D[k] = -D[k];
+            den[k] = -den[k];
+        }
+        fast = fast && den[k] > 0.0f && den[k] < INFINITY;
+    }
+    if (fast) tie |= DG_EDGE_FAST;
+    const float words[16] = {A[0], A[1], A[2], B[0], B[1], B[2], C[0], C[1], C[2], D[0], D[1], D[2],
+                             den[0], den[1], den[2], 0.0f};
+    std::memcpy(w, words, sizeof(words));
+    std::memcpy(w + 15, &tie, 4);
+}
+
+}  // namespace
+
+dg_status dg_canvas_draw_triangles_2d(dg_ctx* c, int32_t canvas, const float* verts, uint32_t n, int32_t texmap,
+                                      const uint64_t* clips) {
+    Canvas* cv = get_canvas(c, canvas);
+    if (!cv || (n && !verts)) return DG_E_INVALID;
+    if (!cv->depth_init) return DG_E_DEPTH_UNINIT;
+    if (texmap < -1 || texmap + 1 >= (int64_t)c->tex.size()) return DG_E_INVALID;
+    if (n == 0) return DG_OK;
+    dg_status e = set_device(c);
+    if (e) return e;
+    e = sync_tex_table(c, c->main.stream);
+    if (e) return e;
+    // host setup (canvas.rs:449-535): snapped centres, bounding box clipped to the
+    // screen and the clipping rectangle, edges, attributes
+    std::vector<DgTriRec> rec(n);
+    std::vector<uint4> box(n);
+    std::vector<unsigned long long> scan(n + 1);
+    const HRect screen = HRect::from_coords(0, 0, cv->w - 1, cv->h - 1);
+    unsigned long long total = 0;
+    for (uint32_t t = 0; t < n; t++) {
+        const float* v = verts + 24ull * t;
+        float cx[3], cy[3], words[28];
+        for (int k = 0; k < 3; k++) {  // pos_map_center, canvas.rs:896-904
+            cx[k] = std::floor(v[8 * k] + 0.5f);
+            cy[k] = std::floor(v[8 * k + 1] + 0.5f);
+        }
+        auto mn = [](float a, float b, float d) {  // NaN-skipping strict-< minimum
+            float r = INFINITY;
+            for (float x : {a, b, d})
+                if (x < r) r = x;
+            return r;
+        };
+        auto mx = [](float a, float b, float d) {
+            float r = -INFINITY;
+            for (float x : {a, b, d})
+                if (x > r) r = x;
+            return r;
+        };
+        const HRect drawable = HRect::clip(
+            HRect::from_coords(h_as_usize(mn(cx[0], cx[1], cx[2])), h_as_usize(mn(cy[0], cy[1], cy[2])),
+                               h_as_usize(mx(cx[0], cx[1], cx[2])), h_as_usize(mx(cy[0], cy[1], cy[2]))),
+            screen);
+        const HRect cr = clips ? HRect::from_coords(clips[4ull * t], clips[4ull * t + 1], clips[4ull * t + 2],
+                                                    clips[4ull * t + 3])
+                               : screen;
+        const HRect valid = HRect::clip(cr, drawable);
+        if (valid.x + valid.w >= cv->w || valid.y + valid.h >= cv->h) return DG_E_INVALID;  // outside the canvas
+        host_edges(cx[0], cy[0], cx[1], cy[1], cx[2], cy[2], words);
+        uint32_t col[3];
+        for (int k = 0; k < 3; k++) {  // Color::Custom([r, g, b]).as_pixel(): b, g, r bytes
+            const float* p = v + 8 * k;
+            if (!(p[4] >= 0.0f && p[4] <= 255.0f && p[5] >= 0.0f && p[5] <= 255.0f && p[6] >= 0.0f && p[6] <= 255.0f))
+                return DG_E_INVALID;
+            col[k] = (uint32_t)(uint8_t)p[6] | ((uint32_t)(uint8_t)p[5] << 8) | ((uint32_t)(uint8_t)p[4] << 16);
+        }
+        const float w4[4] = {v[2], v[10], v[18], v[7]}, w5[4] = {v[3], v[11], v[19], v[15]};
+        std::memcpy(words + 16, w4, 16);
+        std::memcpy(words + 20, w5, 16);
+        std::memcpy(words + 24, col, 12);
+        std::memcpy(words + 27, &v[23], 4);
+        std::memset(&rec[t], 0, sizeof(DgTriRec));
+        std::memcpy(&rec[t], words, sizeof(words));
+        const uint64_t bw = valid.w + 1, bh = valid.h + 1;
+        box[t] = make_uint4((uint32_t)valid.x, (uint32_t)valid.y, (uint32_t)bw, 0u);
+        scan[t] = total;
+        total += bw * bh;
+    }
+    scan[n] = total;
+    if (total >= 0x7FFFFFFFull) return DG_E_LIMIT;
+    JobSlot& S = c->main;
+    OverlaySlot& O = c->overlay;
+    auto need = [&](auto** p, size_t* cap, size_t k) -> dg_status { return grow(S, p, cap, std::max<size_t>(k, 1)); };
+    if ((e = need(&O.d_rec, &O.rec_cap, n)) || (e = need(&O.d_box, &O.box_cap, n)) ||
+        (e = need(&O.d_scan, &O.scan_cap, n + 1)) || (e = need(&O.d_fkey[0], &O.frag_cap[0], total)) ||
+        (e = need(&O.d_fkey[1], &O.frag_cap[1], total)) || (e = need(&O.d_fval[0], &O.frag_cap[2], total)) ||
+        (e = need(&O.d_fval[1], &O.frag_cap[3], total)) ||
+        (e = need(&O.d_hist, &O.hist_cap, 256 * ((total + DG_SORT_TILE - 1) / DG_SORT_TILE))) ||
+        (e = need(&O.d_cnt, &O.cnt_cap, 1)))
+        return e;
+    DG_CUDA(cudaStreamSynchronize(S.stream));  // the scratch may still be read by the previous batch
+    DG_CUDA(cudaMemcpyAsync(O.d_rec, rec.data(), n * sizeof(DgTriRec), cudaMemcpyHostToDevice, S.stream));
+    DG_CUDA(cudaMemcpyAsync(O.d_box, box.data(), n * sizeof(uint4), cudaMemcpyHostToDevice, S.stream));
+    DG_CUDA(cudaMemcpyAsync(O.d_scan, scan.data(), (n + 1) * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                            S.stream));
+    DG_CUDA(cudaMemsetAsync(O.d_cnt, 0, sizeof(unsigned long long), S.stream));
+    DgOverlayJob j;
+    std::memset(&j, 0, sizeof(j));
+    j.rec = O.d_rec;
+    j.box = O.d_box;
+    j.scan = O.d_scan;
+    j.n = n;
+    j.width = (uint32_t)cv->w;
+    j.height = (uint32_t)cv->h;
+    j.colour = cv->d_colour;
+    j.depth = cv->d_depth;
+    const TexMap& tm = c->tex[(size_t)(texmap + 1)];
+    j.tex.words = tm.d_words;
+    j.tex.len = tm.len;
+    j.tex.width = tm.w;
+    j.tex.height = tm.h;
+    j.tex.comps = tm.comps;
+    j.tex.fw = (float)tm.w;
+    j.tex.fh = (float)tm.h;
+    j.tex.small = dg_tex_small(tm.len, tm.w, tm.h);
+    for (int k = 0; k < 2; k++) {
+        j.fkey[k] = O.d_fkey[k];
+        j.fval[k] = O.d_fval[k];
+    }
+    j.fcap = (uint32_t)total;
+    j.hist = O.d_hist;
+    j.cnt = O.d_cnt;
+    j.err = S.d_err;
+    auto bits = [](uint64_t v) {
+        uint32_t b = 0;
+        while (v) {
+            b++;
+            v >>= 1;
+        }
+        return b;
+    };
+    for (uint32_t b = 0; b < bits(n - 1); b += 8) j.sort_shift[j.n_sort++] = b;
+    for (uint32_t b = 0; b < bits(cv->w * cv->h - 1); b += 8) j.sort_shift[j.n_sort++] = 32 + b;
+    if (j.n_sort & 1u) j.sort_shift[j.n_sort++] = 56;  // even pass count: the result lands in buffer 0
+    DG_CUDA(dg_launch_overlay(j, (unsigned)c->nsm * 8u, S.stream));
+    return DG_OK;
+}
+
+dg_status dg_canvas_read_rgba(dg_ctx* c, int32_t id, uint8_t* rgba) {
+    Canvas* cv = get_canvas(c, id);
+    if (!cv || !rgba) return DG_E_INVALID;
+    dg_status e = set_device(c);
+    if (e) return e;
+    const uint64_t n = cv->w * cv->h;
+    JobSlot& S = c->main;
+    e = grow(S, &c->overlay.d_rgba, &c->overlay.rgba_cap, std::max<uint64_t>(n, 1));
+    if (e) return e;
+    DG_CUDA(dg_launch_bgra_to_rgba(cv->d_colour, c->overlay.d_rgba, n, S.stream));
+    DG_CUDA(cudaMemcpyAsync(rgba, c->overlay.d_rgba, n * 4, cudaMemcpyDeviceToHost, S.stream));
+    DG_CUDA(cudaStreamSynchronize(S.stream));
+    return slot_take_errors(S);
 }
 
 dg_status dg_canvas_size(dg_ctx* c, int32_t id, uint64_t* w, uint64_t* h) {

@@ -104,6 +104,29 @@ __device__ __forceinline__ void project_snap(const DgFrameDev& fr, V3 p, float& 
     cy = floorf(fA(sy, 0.5f));
 }
 
+// A vertex as the raster setup uses it: snapped screen centre, eye distance
+// (scene/mod.rs:924) and the plane-sign mask of k_vertex, for a job vertex at
+// world position p.
+__device__ __forceinline__ float4 vertex_screen(const DgFrameDev& fr, float4 p4, uint32_t mask) {
+    const V3 p = {p4.x, p4.y, p4.z};
+    const V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
+    const float depth = vnorm(vsub(p, cam));
+    float cx, cy;
+    project_snap(fr, p, cx, cy);
+    return make_float4(cx, cy, depth, __uint_as_float(mask));
+}
+
+// The three vertices of triangle tp of segment sg (vertex_screen of each).
+__device__ __forceinline__ void triangle_vertices(const DgJobDev& job, const DgSegDev& sg, const DgFrameDev& fr,
+                                                  uint4 tp, float4 r[3]) {
+    const float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
+    const uint16_t* vm = job.vmask + sg.vtx_begin;
+    const uint32_t ma = __ldg(vm + tp.x), mb = __ldg(vm + tp.y), mc = __ldg(vm + tp.z);
+    r[0] = vertex_screen(fr, pa, ma);
+    r[1] = vertex_screen(fr, pb, mb);
+    r[2] = vertex_screen(fr, pc, mc);
+}
+
 // ------------------------------------------------------------ edge set
 // f_xy(x, y) = (((p.y - q.y) * x + (q.x - p.x) * y) + p.x * q.y) - q.x * p.y
 // (canvas.rs:597-616) with the per-edge constants precomputed; the per-pixel
@@ -130,6 +153,24 @@ __device__ __forceinline__ void make_edges(float ax, float ay, float bx, float b
         float out = edge_eval(e, k, -1.0f, -1.0f);
         if (fM(e.den[k], out) > 0.0f) e.tie |= 1u << k;
     }
+    // Normalization: an edge whose f_alpha (den) has its sign bit set is negated
+    // as a whole (A, B, C, D and den). Round-to-nearest is symmetric in sign, so
+    // the negated constants give exactly -f at every pixel, and f/den, the tie
+    // product den * f(-1,-1) and every result derived from them are
+    // bit-identical; only the signs that the coverage test compares change.
+    bool fast = true;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        if (signbit(e.den[k])) {
+            e.A[k] = -e.A[k];
+            e.B[k] = -e.B[k];
+            e.C[k] = -e.C[k];
+            e.D[k] = -e.D[k];
+            e.den[k] = -e.den[k];
+        }
+        fast = fast && e.den[k] > 0.0f && e.den[k] < INFINITY;
+    }
+    if (fast) e.tie |= DG_EDGE_FAST;
 }
 
 // Division-free early reject, exact with respect to the reference's test.
@@ -154,10 +195,25 @@ __device__ __forceinline__ bool covered_divide(const EdgeSet& e, float n0, float
     if (!(al >= 0.0f && be >= 0.0f && ga >= 0.0f)) return false;
     return (al > 0.0f || (e.tie & 1u)) && (be > 0.0f || (e.tie & 2u)) && (ga > 0.0f || (e.tie & 4u));
 }
+// The coverage test of an edge set with DG_EDGE_FAST (every den finite and
+// > 0 after normalization), without division: alpha = n0 / den0 is >= 0 exactly
+// when n0 >= 0 (NaN fails both), and > 0 exactly when n0 > 0 (an integer-valued
+// n0 >= 1 over a finite den cannot underflow to zero); likewise beta, gama.
+__device__ __forceinline__ bool covered_signs(uint32_t tie, float n0, float n1, float n2) {
+    return (n0 > 0.0f || (n0 == 0.0f && (tie & 1u))) && (n1 > 0.0f || (n1 == 0.0f && (tie & 2u))) &&
+           (n2 > 0.0f || (n2 == 0.0f && (tie & 4u)));
+}
 __device__ __forceinline__ bool covered(const EdgeSet& e, float x, float y, float& al, float& be, float& ga) {
     const float n0 = edge_eval(e, 0, x, y);
     const float n1 = edge_eval(e, 1, x, y);
     const float n2 = edge_eval(e, 2, x, y);
+    if (e.tie & DG_EDGE_FAST) {
+        if (!covered_signs(e.tie, n0, n1, n2)) return false;
+        al = fD(n0, e.den[0]);
+        be = fD(n1, e.den[1]);
+        ga = fD(n2, e.den[2]);
+        return true;
+    }
     if (prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2])) return false;
     return covered_divide(e, n0, n1, n2, al, be, ga);
 }
@@ -672,7 +728,7 @@ __device__ __noinline__ uint32_t shade_without_record(const DgJobDev& job, const
     const uint32_t ui[3] = {tuv.x, tuv.y, tuv.z};
     const uint32_t ni[3] = {tnr.x, tnr.y, tnr.z};
     float4 r[3];
-    for (int k = 0; k < 3; k++) r[k] = __ldg(job.vrec + sg.vtx_begin + vi[k]);
+    triangle_vertices(job, sg, fr, tp, r);
     uint32_t gt = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
     const bool clipped = (gt & 0x3u) != 0x3u;
     ClipProg P;

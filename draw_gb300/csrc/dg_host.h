@@ -111,8 +111,8 @@ struct FrameTarget {
 // one; the render server owns one per concurrent batch.
 struct JobSlot {
     cudaStream_t stream = nullptr;
-    float4* d_vrec = nullptr;
-    size_t vrec_cap = 0;
+    uint16_t* d_vmask = nullptr;  // plane-sign masks of the job's vertices
+    size_t vmask_cap = 0;
     float4* d_vshade = nullptr;
     size_t vshade_cap = 0;
     uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
@@ -171,6 +171,27 @@ struct JobSlot {
 
 }  // namespace dgh
 
+namespace dgh {
+// Scratch of dg_canvas_draw_triangles_2d (grow-only, on the context stream).
+struct OverlaySlot {
+    DgTriRec* d_rec = nullptr;
+    size_t rec_cap = 0;
+    uint4* d_box = nullptr;
+    size_t box_cap = 0;
+    unsigned long long* d_scan = nullptr;
+    size_t scan_cap = 0;
+    uint64_t* d_fkey[2] = {};
+    uint32_t* d_fval[2] = {};
+    size_t frag_cap[4] = {};
+    uint32_t* d_hist = nullptr;
+    size_t hist_cap = 0;
+    unsigned long long* d_cnt = nullptr;
+    size_t cnt_cap = 0;
+    uint32_t* d_rgba = nullptr;  // staging of dg_canvas_read_rgba
+    size_t rgba_cap = 0;
+};
+}  // namespace dgh
+
 struct dg_ctx {
     int device = 0;
     int nsm = 152;
@@ -183,6 +204,7 @@ struct dg_ctx {
     std::vector<dgh::Scene> scenes;
     std::vector<dgh::Canvas> canvases;
     dgh::JobSlot main;  // the slot of dg_scene_render / dg_render_batch (main.stream = the context stream)
+    dgh::OverlaySlot overlay;
 };
 
 namespace dgh {

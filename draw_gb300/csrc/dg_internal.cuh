@@ -9,8 +9,8 @@
 //   canvas        : colour u32[W*H] (BGRA bytes, row 0 = top), depth f32[W*H]
 //                   (y*W+x, y = 0 at the bottom), vis u64[W*H] (visibility keys,
 //                   kept at DG_VIS_EMPTY between frames)
-//   render scratch: vrec float4[V_total] (snapped centre x,y, eye distance,
-//                   plane-sign masks), vshade float4[V_total*L*2] (light, halfway),
+//   render scratch: vmask u16[V_total] (plane-sign masks of each vertex),
+//                   vshade float4[V_total*L*2] (light, halfway),
 //                   raster-queue records + their work-unit bases, counters
 #pragma once
 
@@ -90,7 +90,7 @@ static_assert(offsetof(DgFrameDev, plane) == 64 && offsetof(DgFrameDev, cam) == 
 struct DgSegDev {
     uint32_t frame;
     uint32_t tri_begin;  // job-wide index of the segment's first triangle
-    uint32_t vtx_begin;  // job-wide index of the segment's first vertex (vrec/vshade row)
+    uint32_t vtx_begin;  // job-wide index of the segment's first vertex (vmask/vshade row)
     uint32_t seq_base;   // frame-local submission index of the first triangle
     uint32_t ntri, nv;
     uint32_t nmats, pad;
@@ -120,8 +120,12 @@ struct DgSegDev {
 struct DgEdges {
     float A[3], B[3], C[3], D[3];
     float den[3];  // f_alpha = f_bc(a), f_beta = f_ca(b), f_gama = f_ab(c)
-    uint32_t tie;  // bit k: den[k] * f_k(-1, -1) > 0 (the reference's tie rule)
+    uint32_t tie;  // bit k: den[k] * f_k(-1, -1) > 0 (the reference's tie rule); DG_EDGE_FAST
 };
+
+// Set in DgEdges.tie when every den is finite and > 0 (edges are stored
+// normalized to a den without sign bit): coverage is then a sign test.
+#define DG_EDGE_FAST 8u
 
 // One triangle (or one clip output of it) as the raster and shade passes read
 // it: twelve 16-byte words. Attribute fields hold the three vertices' values
@@ -177,7 +181,7 @@ struct DgJobDev {
     uint32_t nframes, nsegs;
     uint32_t total_vtx, total_tri, total_tiles;
     uint32_t shade_stride;  // lights per row of vshade (max over frames)
-    float4* vrec;
+    uint16_t* vmask;        // [total_vtx] bit p: plane p has f > 0; bit 8 + p: f <= 0 (near, far, 4 lateral)
     float4* vshade;         // rows [0, total_vtx): job vertices; then rows for clip vertices
     uint32_t vrow_extra;    // rows after total_vtx available to clip vertices
     uint32_t* vmark;        // one bit per job vertex: needs light/halfway vectors (kept zero between jobs)
@@ -247,6 +251,31 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
 // transparent setup), part 1 after the opaque raster (fragment emission and
 // sort), part 2 after the opaque resolve (the ordered blend).
 cudaError_t dg_launch_transparent(int part, const DgJobDev& job, const DgTransparentPlan& plan, cudaStream_t s);
+
+// One batch of 2D overlay triangles (Canvas::draw_triangle, canvas.rs:435-575)
+// drawn into one canvas in order. The host sets every triangle up (snapped
+// centres, clipped bounding box, edges, attributes in rec words 4-6: u, v, the
+// vertex colours as packed BGR0 words, the vertex alphas in the w slots) and the
+// prefix sums of the boxes' pixels; the GPU rasterizes, sorts the fragments by
+// (pixel, triangle) and blends each pixel's fragments in order.
+struct DgOverlayJob {
+    const DgTriRec* rec;              // [n]
+    const uint4* box;                 // [n] (x_min, y_min, width, 0)
+    const unsigned long long* scan;   // [n + 1] exclusive prefix sums of the boxes' pixels
+    uint32_t n;
+    uint32_t width, height;
+    uint32_t* colour;                 // the canvas (BGRA, row 0 = top)
+    const float* depth;               // y*W+x
+    DgTexDev tex;                     // the RGBA map
+    uint64_t* fkey[2];                // fragment keys (pixel << 32 | triangle) and triangles
+    uint32_t* fval[2];
+    uint32_t fcap;
+    uint32_t* hist;
+    unsigned long long* cnt;          // [0] fragments emitted
+    uint32_t* err;
+    uint32_t sort_shift[8], n_sort;
+};
+cudaError_t dg_launch_overlay(const DgOverlayJob& job, unsigned blocks, cudaStream_t s);
 // Scratch rows and records sized for a job of T triangles (shared sizing rule).
 constexpr uint64_t dg_trec_cap(uint64_t T) { return T + T / 8u + 4096u; }
 constexpr uint64_t dg_items_cap(uint64_t queue_cap) { return 2u * queue_cap + 65536u; }
@@ -254,6 +283,7 @@ constexpr uint64_t dg_vrow_extra(uint64_t T) { uint64_t x = 65536u + T / 8u; ret
 cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t colour_value, float depth_value,
                            int fill_colour, int fill_depth, cudaStream_t s);
 cudaError_t dg_launch_vis_reset(uint64_t* vis, uint64_t n, cudaStream_t s);
+cudaError_t dg_launch_bgra_to_rgba(const uint32_t* src, uint32_t* dst, uint64_t n, cudaStream_t s);
 
 // Host frame setup without a context (dg_api.cu).
 dg_status dg_host_frame_setup(uint64_t width, uint64_t height, const float pos[3], const float dir[3], float ratio,

@@ -42,10 +42,6 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
         const DgFrameDev& fr = job.frames[sg.frame];
         float4 p4 = __ldg(sg.pos + (v - sg.vtx_begin));
         V3 p = {p4.x, p4.y, p4.z};
-        V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
-        float depth = vnorm(vsub(p, cam));  // eye distance, scene/mod.rs:924
-        float cx, cy;
-        project_snap(fr, p, cx, cy);
         uint32_t mask = 0;
 #pragma unroll
         for (int pl = 0; pl < 6; pl++) {
@@ -53,7 +49,7 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
             if (f > 0.0f) mask |= 1u << pl;
             if (f <= 0.0f) mask |= 1u << (8 + pl);
         }
-        job.vrec[v] = make_float4(cx, cy, depth, __uint_as_float(mask));
+        job.vmask[v] = (uint16_t)mask;
     }
 }
 
@@ -77,9 +73,8 @@ __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
             const uint32_t si = seg_of_tri(job, g);
             const DgSegDev& sg = job.segs[si];
             const uint4 tp = __ldg(sg.tri_pos + (g - sg.tri_begin));
-            const float* mw = reinterpret_cast<const float*>(job.vrec + sg.vtx_begin) + 3;
-            const uint32_t m = __float_as_uint(__ldg(mw + 4ull * tp.x)) & __float_as_uint(__ldg(mw + 4ull * tp.y)) &
-                               __float_as_uint(__ldg(mw + 4ull * tp.z));
+            const uint16_t* vm = job.vmask + sg.vtx_begin;
+            const uint32_t m = (uint32_t)__ldg(vm + tp.x) & (uint32_t)__ldg(vm + tp.y) & (uint32_t)__ldg(vm + tp.z);
             if (((m >> 8) & 0x3Du) == 0u) {
                 const float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
                 const V3 a = {pa.x, pa.y, pa.z}, b = {pb.x, pb.y, pb.z}, c = {pc.x, pc.y, pc.z};
@@ -129,9 +124,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             tp = __ldg(sg.tri_pos + t);
             tuv = __ldg(sg.tri_uv + t);  // for the triangle record, loaded alongside the vertex records
             tnr = __ldg(sg.tri_nrm + t);
-            r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
-            r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
-            r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
+            triangle_vertices(job, sg, job.frames[sg.frame], tp, r);
             const uint32_t m = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
             if ((m & 0x3u) == 0x3u) {
                 nout = 1;  // inside near and far: the triangle passes unchanged
@@ -344,7 +337,17 @@ __device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uin
                                                 float clear_depth, unsigned long long* vis, uint32_t width) {
     float al, be, ga;
     const float xf = (float)x, yf = (float)y;
-    if (covered_divide(e, edge_eval(e, 0, xf, yf), edge_eval(e, 1, xf, yf), edge_eval(e, 2, xf, yf), al, be, ga)) {
+    const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
+    bool cov;
+    if (e.tie & DG_EDGE_FAST) {  // the candidate passed the sign test: only the barycentrics remain
+        al = fD(n0, e.den[0]);
+        be = fD(n1, e.den[1]);
+        ga = fD(n2, e.den[2]);
+        cov = true;
+    } else {
+        cov = covered_divide(e, n0, n1, n2, al, be, ga);
+    }
+    if (cov) {
         const float depth = interp(al, be, ga, dd.x, dd.y, dd.z);
         if (depth < clear_depth) atomicMin(vis + (uint64_t)y * width + x, depth_key(depth, seq));
     }
@@ -411,20 +414,27 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
         // them (the reference's full test with its three divisions, then the
         // depth key), so the division path runs with all lanes busy.
         uint32_t pending = 0;
+        const bool fast = (e.tie & DG_EDGE_FAST) != 0u;
         for (uint32_t u = item.y; u < u_end; u++) {
-            const uint32_t k = u * DG_UNIT_PX + lane;
+            // the unit's first pixel: k0 / w from a float reciprocal, corrected to the exact quotient
+            const uint32_t k0 = u * DG_UNIT_PX;
+            uint32_t y0 = (uint32_t)__fmul_rz((float)k0, rcp_w);
+            while ((uint64_t)y0 * w > k0) y0--;
+            while ((uint64_t)(y0 + 1u) * w <= k0) y0++;
+            // this lane's pixel, k0 + lane, by stepping along the rows
+            uint32_t xx = (k0 - y0 * w) + lane, yy = y0;
+            if (xx >= w) {
+                const uint32_t q = w >= DG_UNIT_PX ? 1u : xx / w;
+                xx -= q * w;
+                yy += q;
+            }
             bool cand = false;
-            uint32_t x = 0, y = 0;
-            if (k < npx) {
-                // k / w from a float reciprocal, corrected to the exact quotient
-                uint32_t yy = (uint32_t)__fmul_rz((float)k, rcp_w);
-                while ((uint64_t)yy * w > k) yy--;
-                while ((uint64_t)(yy + 1u) * w <= k) yy++;
-                x = xlo + (k - yy * w);
-                y = ylo + yy;
+            const uint32_t x = xlo + xx, y = ylo + yy;
+            if (k0 + lane < npx) {
                 const float xf = (float)x, yf = (float)y;
-                cand = !(prereject(edge_eval(e, 0, xf, yf), e.den[0]) || prereject(edge_eval(e, 1, xf, yf), e.den[1]) ||
-                         prereject(edge_eval(e, 2, xf, yf), e.den[2]));
+                const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
+                cand = fast ? covered_signs(e.tie, n0, n1, n2)
+                            : !(prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2]));
             }
             const unsigned b = __ballot_sync(FULL, cand);
             if (cand) {
@@ -631,6 +641,15 @@ __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, 
     }
 }
 
+// The RGBA view of a BGRA frame: bytes 0 and 2 of every pixel swapped, the
+// fourth byte kept (Application::export_frame_as, app/mod.rs:345-350).
+__global__ void k_bgra_to_rgba(const uint32_t* src, uint32_t* dst, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = src[i];
+        dst[i] = (s & 0xFF00FF00u) | ((s >> 16) & 0xFFu) | ((s & 0xFFu) << 16);
+    }
+}
+
 __global__ void k_vis_reset(uint64_t* vis, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         vis[i] = DG_VIS_EMPTY;
@@ -684,6 +703,12 @@ cudaError_t dg_launch_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t 
                            int fill_colour, int fill_depth, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_fill<<<grid_for(n, 4096u), 256, 0, s>>>(colour, depth, n, colour_value, depth_value, fill_colour, fill_depth);
+    return cudaGetLastError();
+}
+
+cudaError_t dg_launch_bgra_to_rgba(const uint32_t* src, uint32_t* dst, uint64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_bgra_to_rgba<<<grid_for(n, 4096u), 256, 0, s>>>(src, dst, n);
     return cudaGetLastError();
 }
 

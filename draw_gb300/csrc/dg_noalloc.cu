@@ -33,7 +33,7 @@ constexpr size_t kOffDesc = 0;
 constexpr uint32_t kVrowExtra = 4096;  // light/halfway rows for clip vertices
 constexpr uint32_t kTrecCap = (uint32_t)dg_trec_cap(DG_NOALLOC_MAX_TRIANGLES);  // triangle records
 constexpr size_t kOffVrec = align_up(kOffDesc + sizeof(NoallocDesc));
-constexpr size_t kOffVshade = align_up(kOffVrec + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(float4));
+constexpr size_t kOffVshade = align_up(kOffVrec + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(uint16_t));
 constexpr size_t kOffVmark = align_up(kOffVshade + (size_t)(DG_NOALLOC_MAX_VERTICES + kVrowExtra) *
                                                        DG_NOALLOC_MAX_LIGHTS * 2 * sizeof(float4));
 constexpr size_t kOffQueue = align_up(kOffVmark + (size_t)(DG_NOALLOC_MAX_VERTICES / 32) * sizeof(uint32_t));
@@ -201,7 +201,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.total_tiles = tiles;
     job.fb_tiles = reinterpret_cast<uint32_t*>(base + kOffFb);
     job.shade_stride = p->nlights;
-    job.vrec = reinterpret_cast<float4*>(base + kOffVrec);
+    job.vmask = reinterpret_cast<uint16_t*>(base + kOffVrec);
     job.vshade = reinterpret_cast<float4*>(base + kOffVshade);
     job.vrow_extra = kVrowExtra;
     job.vmark = reinterpret_cast<uint32_t*>(base + kOffVmark);

@@ -1,6 +1,7 @@
 // dg_transparent.cu -- the transparent pass of Scene::render on the GPU
 // (scene/mod.rs:1088-1247 with canvas.rs:906-930 and the Pixel arithmetic of
-// canvas.rs:136-169).
+// canvas.rs:136-169), and the 2D overlay triangles of Canvas::draw_triangle
+// (canvas.rs:435-575), the other order-dependent blend of the reference.
 //
 // In the reference, each object draws its opaque meshes with depth writes on,
 // then its transparent meshes with depth writes off: every transparent mesh is
@@ -237,9 +238,7 @@ __global__ void __launch_bounds__(256) k_tsetup(const DgJobDev job) {
         const uint32_t loc = j - sg.t_begin;
         const uint4 tp = __ldg(sg.tdst[0] + loc), tuv = __ldg(sg.tdst[1] + loc), tnr = __ldg(sg.tdst[2] + loc);
         float4 r[3];
-        r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
-        r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
-        r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
+        triangle_vertices(job, sg, fr, tp, r);
         const uint32_t m = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
         const uint32_t rowbase = job.total_vtx + job.vrow_extra + 6u * j;
         ClipProg P;
@@ -432,7 +431,131 @@ __global__ void __launch_bounds__(256) k_tfold(const DgJobDev job) {
     }
 }
 
+// ------------------------------------------------------------ 2D overlay
+// Canvas::draw_triangle (canvas.rs:435-575): every pixel of every clipped
+// bounding box and the coverage test (the same edge functions and tie rule as
+// the 3D rasterizer); covered pixels become fragments.
+__global__ void __launch_bounds__(256) k_o_raster(const DgOverlayJob job) {
+    wait_previous_kernel();
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long total = job.scan[job.n];
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total;
+         base += stride) {
+        const unsigned long long q = base + lane;
+        bool emit = false;
+        uint32_t tri = 0, px = 0;
+        if (q < total) {
+            uint32_t lo = 0, hi = job.n;  // largest t with scan[t] <= q
+            while (hi - lo > 1u) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__ldg(job.scan + mid) <= q)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            tri = lo;
+            const uint32_t k = (uint32_t)(q - __ldg(job.scan + tri));
+            const uint4 box = __ldg(job.box + tri);
+            const uint32_t y = box.y + k / box.z, x = box.x + k % box.z;
+            EdgeSet e;
+            load_edges(job.rec + tri, e);
+            float al, be, ga;
+            if (covered(e, (float)x, (float)y, al, be, ga)) {
+                emit = true;
+                px = y * job.width + x;
+            }
+        }
+        const unsigned em = __ballot_sync(0xFFFFFFFFu, emit);
+        if (em) {
+            const int leader = __ffs(em) - 1;
+            unsigned long long slot = 0;
+            if ((int)lane == leader) slot = atomicAdd(job.cnt, (unsigned long long)__popc(em));
+            slot = __shfl_sync(0xFFFFFFFFu, slot, leader) + __popc(em & ((1u << lane) - 1u));
+            if (emit && slot < job.fcap) {
+                job.fkey[0][slot] = ((uint64_t)px << 32) | tri;
+                job.fval[0][slot] = tri;
+            }
+        }
+    }
+}
+
+// TextureMap::get_rgba_slice (scene/mod.rs:137-152): (u * width) and
+// (v * height) floored, wrapping usize offset, four bytes; false where the
+// reference's slice index would panic.
+__device__ __forceinline__ bool tex_rgba(const DgTexDev& tx, float u, float v, uint32_t& rgba) {
+    const uint64_t ui = as_usize(floorf(fM(u, tx.fw)));
+    const uint64_t vi = (uint64_t)tx.height - 1ull - as_usize(floorf(fM(v, tx.fh)));
+    const uint64_t off = (vi * (uint64_t)tx.width + ui) * (uint64_t)tx.comps;
+    if (tx.len < 4ull || off > tx.len - 4ull) return false;
+    const uint64_t w = off >> 2;
+    const uint32_t sh = (uint32_t)(off & 3ull) * 8u;
+    const uint32_t lo = __ldg(tx.words + w);
+    rgba = sh == 0u ? lo : __funnelshift_r(lo, __ldg(tx.words + w + 1), sh);
+    return true;
+}
+
+// Each pixel's fragments in triangle order: the vertex colours and alphas and
+// the texture coordinates interpolated with the barycentrics, the RGBA texel,
+// the colour blend with the texel, and draw_pixel_coord_with_depth's depth test
+// at depth 0 (the overlay never writes depth: depth updates are off outside the
+// opaque pass) and blend with the canvas (canvas.rs:529-573, 906-930).
+__global__ void __launch_bounds__(256) k_o_fold(const DgOverlayJob job) {
+    wait_previous_kernel();
+    const unsigned long long n64 = *job.cnt;
+    const uint32_t n = (uint32_t)(n64 < job.fcap ? n64 : job.fcap);
+    if (threadIdx.x == 0 && blockIdx.x == 0 && n64 > job.fcap) atomicOr(job.err, 1u << DG_E_LIMIT);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t p = (uint32_t)(job.fkey[0][i] >> 32);
+        if (i > 0u && (uint32_t)(job.fkey[0][i - 1u] >> 32) == p) continue;  // not the pixel's first
+        const uint32_t y = p / job.width, x = p - y * job.width;
+        const uint64_t ci = (uint64_t)(job.height - 1u - y) * job.width + x;
+        const bool pass = 0.0f < job.depth[(uint64_t)y * job.width + x];
+        uint32_t bg = job.colour[ci];
+        uint32_t bits = 0;
+        for (uint32_t m = i; m < n && (uint32_t)(job.fkey[0][m] >> 32) == p; m++) {
+            const DgTriRec* R = job.rec + job.fval[0][m];
+            EdgeSet e;
+            load_edges(R, e);
+            float al, be, ga;
+            covered(e, (float)x, (float)y, al, be, ga);  // the fragment passed it in k_o_raster
+            const float4* q = reinterpret_cast<const float4*>(R);
+            const float4 fu = __ldg(q + 4), fv = __ldg(q + 5);
+            const uint4 fc = __ldg(reinterpret_cast<const uint4*>(R) + 6);
+            // (alpha * color_a) + (beta * color_b) + (gama * color_c): Pixel products and sums
+            const uint32_t cp0 = px_add(px_add(px_mul(fc.x, al), px_mul(fc.y, be)), px_mul(fc.z, ga));
+            const float calpha = fA(fA(fM(al, fu.w), fM(be, fv.w)), fM(ga, __uint_as_float(fc.w)));
+            const float cu = fA(fA(fM(fu.x, al), fM(fu.y, be)), fM(fu.z, ga));
+            const float cv = fA(fA(fM(fv.x, al), fM(fv.y, be)), fM(fv.z, ga));
+            uint32_t rgba;
+            if (!tex_rgba(job.tex, cu, cv, rgba)) {
+                bits |= 1u << DG_E_TEXTURE_RANGE;
+                continue;
+            }
+            const float talpha = fD((float)(rgba >> 24), 255.0f);
+            const uint32_t ct = ((rgba >> 16) & 0xFFu) | (((rgba >> 8) & 0xFFu) << 8) | ((rgba & 0xFFu) << 16);
+            const uint32_t cp = px_add(px_mul(cp0, talpha), px_mul(ct, fS(1.0f, talpha)));
+            const float fa = fM(calpha, talpha);
+            if (pass) bg = fa < 1.0f ? px_add(px_mul(bg, fS(1.0f, fa)), px_mul(cp, fa)) : cp;
+        }
+        job.colour[ci] = bg;
+        if (bits) atomicOr(job.err, bits);
+    }
+}
+
 }  // namespace
+
+cudaError_t dg_launch_overlay(const DgOverlayJob& job, unsigned blocks, cudaStream_t s) {
+    if (job.n == 0u) return cudaSuccess;
+    const unsigned g = blocks < 1u ? 1u : blocks;
+    cudaError_t e = launch_dependent(k_o_raster, g, 256, job, s);
+    if (e != cudaSuccess) return e;
+    if ((e = radix_sort(job.fkey, job.fval, job.hist, job.cnt, job.fcap, job.sort_shift, job.n_sort, g, s)) !=
+        cudaSuccess)
+        return e;
+    return launch_dependent(k_o_fold, g, 256, job, s);
+}
 
 cudaError_t dg_launch_transparent(int part, const DgJobDev& job, const DgTransparentPlan& plan, cudaStream_t s) {
     if (job.ntt == 0u) return cudaSuccess;

@@ -62,6 +62,8 @@ SIGNATURES = {
     "dg_canvas_write": (_i32, [_P, _i32, _P, _P]),
     "dg_canvas_device_ptrs": (_i32, [_P, _i32, _P, _P]),
     "dg_canvas_size": (_i32, [_P, _i32, _P, _P]),
+    "dg_canvas_draw_triangles_2d": (_i32, [_P, _i32, _P, _u32, _i32, _P]),
+    "dg_canvas_read_rgba": (_i32, [_P, _i32, _P]),
     "dg_scene_render": (_i32, [_P, _i32, _i32]),
     "dg_render_batch": (_i32, [_P, _P, _P, _u32]),
     "dg_render_noalloc": (_i32, [_P, _P, _P, _u32, _P, _u32, _P, _P, _P, _P]),
@@ -70,6 +72,13 @@ SIGNATURES = {
     "dg_batch_info": (_i32, [_P, _P, _i32]),
     "dg_batch_destroy": (_i32, [_P]),
     "dg_autotune": (_i32, [_P, _P, _P, _u32, _u32, _P, _P]),
+    "dg_obj_parse": (_i32, [ctypes.c_char_p, _P]),
+    "dg_obj_counts": (_i32, [_P, _P, _i32]),
+    "dg_obj_arrays": (_i32, [_P, _P, _P, _P]),
+    "dg_obj_mesh": (_i32, [_P, _u64, _P, _u64, _P, _P, _P, _u64]),
+    "dg_obj_material": (_i32, [_P, _u64, _P, _P, _u64, _P, _P, _u64]),
+    "dg_obj_name": (_i32, [_P, _P, _u64]),
+    "dg_obj_free": (_i32, [_P]),
     "dg_server_create": (_i32, [_P, _u64, _u32, _u32, _P]),
     "dg_server_submit": (_i32, [_P, _P, _P]),
     "dg_server_wait": (_i32, [_P, _u64, _P, _P, _P]),
@@ -302,6 +311,16 @@ class TextureMap:
         self.id = out.value
         self.width, self.height, self.components = width, height, components
 
+    @staticmethod
+    def load_from_file(path: str, ctx: Context | None = None) -> "TextureMap":
+        """TextureMap::load_from_file (scene/mod.rs:174-202): 3- or 4-component images only."""
+        from . import imageio
+
+        img, w, h, comps = imageio.read_image(path)
+        if comps not in (3, 4):
+            raise DrawError(1, f"TextureMap::load_from_file {path}: {comps} components")
+        return TextureMap(img, w, h, comps, ctx)
+
 
 @dataclass
 class Texture:
@@ -384,6 +403,57 @@ class Object:
         self.meshes = meshes
         self.textures = textures
 
+    @staticmethod
+    def load_from_file(filename: str, ctx: Context | None = None) -> "Object":
+        """Object::load_from_file (object.rs:106-454): the OBJ file and its MTL
+        libraries parsed by the library (dg_obj_*), texture maps decoded here."""
+        ctx = ctx or default_context()
+        lib = ctx.lib
+        h = ctypes.c_void_p()
+        _chk(lib.dg_obj_parse(os.fsencode(filename), ctypes.byref(h)), f"Object::load_from_file {filename}")
+        try:
+            cnt = (ctypes.c_uint64 * 6)()
+            _chk(lib.dg_obj_counts(h, cnt, 6), "obj counts")
+            nv, nn, nuv, nmesh, nmat = (int(x) for x in cnt[:5])
+            v = np.zeros((nv, 3), np.float32)
+            n = np.zeros((nn, 3), np.float32)
+            uv = np.zeros((nuv, 3), np.float32)
+            _chk(lib.dg_obj_arrays(h, _ptr(v), _ptr(n), _ptr(uv)), "obj arrays")
+            name = ctypes.create_string_buffer(1024)
+            meshes = []
+            for i in range(nmesh):
+                nt, ti = ctypes.c_uint64(), ctypes.c_int32()
+                _chk(lib.dg_obj_mesh(h, i, None, 0, ctypes.byref(nt), ctypes.byref(ti), name, 1024), "obj mesh")
+                t = np.zeros((nt.value, 9), np.uint32)
+                _chk(lib.dg_obj_mesh(h, i, _ptr(t), t.size, ctypes.byref(nt), ctypes.byref(ti), name, 1024),
+                     "obj mesh")
+                meshes.append(IndexedMesh(name.value.decode(), t, ti.value))
+            maps: dict = {}
+            textures = []
+            pa, pd = ctypes.create_string_buffer(4096), ctypes.create_string_buffer(4096)
+            for i in range(nmat):
+                m = dg_material()
+                _chk(lib.dg_obj_material(h, i, ctypes.byref(m), name, 1024, pa, pd, 4096), "obj material")
+                tm = []
+                for p in (pa.value.decode(), pd.value.decode()):
+                    if p and p not in maps:
+                        maps[p] = TextureMap.load_from_file(p, ctx)
+                    tm.append(maps[p] if p else None)
+                textures.append(Texture(name.value.decode(), tuple(m.ka), tuple(m.kd), tuple(m.ks), m.alpha, tm[0],
+                                        tm[1]))
+            _chk(lib.dg_obj_name(h, name, 1024), "obj name")
+            return Object(name.value.decode(), v, n, uv, meshes, textures, ctx)
+        finally:
+            lib.dg_obj_free(h)
+
+    @staticmethod
+    def load_from_directory(directory: str, ctx: Context | None = None) -> list:
+        """Object::load_from_directory (object.rs:73-103): every .obj file of the directory."""
+        if not os.path.isdir(directory):
+            return []
+        return [Object.load_from_file(os.path.join(directory, f), ctx) for f in sorted(os.listdir(directory))
+                if f.endswith(".obj") and os.path.isfile(os.path.join(directory, f))]
+
     def transparent_triangles(self, mesh: int) -> np.ndarray:
         """The current (painter's sort) order of transparent mesh `mesh` as (T, 9)
         indices; Scene::render re-sorts it every frame and keeps it (scene/mod.rs:1100-1115)."""
@@ -397,11 +467,11 @@ class Object:
         return out
 
     def mesh_info_list(self) -> list:  # object.rs:456-476 (opaque meshes first, then transparent)
-        op = [m for m in self.meshes if self.textures[m.texture_idx].alpha >= 1.0 or
-              np.isnan(self.textures[m.texture_idx].alpha)]
-        tr = [m for m in self.meshes if m not in op]
+        transparent = [self.textures[m.texture_idx].alpha < 1.0 for m in self.meshes]
+        order = [m for m, t in zip(self.meshes, transparent) if not t] + \
+                [m for m, t in zip(self.meshes, transparent) if t]
         return [MeshInfo(m.name, int(np.asarray(m.triangles).reshape(-1, 9).shape[0]),
-                         self.textures[m.texture_idx].name) for m in op + tr]
+                         self.textures[m.texture_idx].name) for m in order]
 
 
 class Camera:
@@ -520,6 +590,33 @@ class Canvas:
         d = np.empty((self.height, self.width), np.float32) if depth else None
         _chk(self.ctx.lib.dg_canvas_read(self.ctx.h, self.id, _ptr(bgra), _ptr(d)), "Canvas::read")
         return bgra, d
+
+    def read_rgba(self) -> np.ndarray:
+        """(H, W, 4) RGBA bytes, row 0 = top: the frame Application::export_frame_as writes."""
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        _chk(self.ctx.lib.dg_canvas_read_rgba(self.ctx.h, self.id, _ptr(out)), "read_rgba")
+        return out
+
+    def export_frame_as(self, path: str):
+        """Application::export_frame_as (app/mod.rs:316-379): PNG with 4 components
+        (the padding byte as alpha), or binary PPM (RGB); JPEG is not encoded here."""
+        from . import imageio
+
+        if path.lower().endswith(".png"):
+            imageio.write_png(path, self.read_rgba())
+        elif path.lower().endswith(".ppm"):
+            imageio.write_ppm(path, self.read_rgba())
+        else:
+            raise DrawError(1, f"export_frame_as {path}: PNG and PPM are written")
+
+    def draw_triangles(self, verts, texture_map: "TextureMap | None" = None, clips=None):
+        """Canvas::draw_triangle (canvas.rs:435-575) for n triangles in order: verts
+        (n, 3, 8) = (x, y, u, v, r, g, b, alpha) per vertex; clips (n, 4) or None."""
+        v = np.ascontiguousarray(verts, np.float32).reshape(-1, 24)
+        c = None if clips is None else np.ascontiguousarray(clips, np.uint64).reshape(-1, 4)
+        tid = texture_map.id if texture_map is not None else -1
+        _chk(self.ctx.lib.dg_canvas_draw_triangles_2d(self.ctx.h, self.id, _ptr(v), v.shape[0], tid, _ptr(c)),
+             "Canvas::draw_triangle")
 
     def read_into(self, bgra: np.ndarray, depth: np.ndarray | None):
         _chk(self.ctx.lib.dg_canvas_read(self.ctx.h, self.id, _ptr(bgra), _ptr(depth)), "Canvas::read")

@@ -127,6 +127,34 @@ dg_status dg_object_create(dg_ctx* ctx, const float* vertices, uint64_t nv, cons
                            const dg_material* materials, uint64_t nmat, int32_t* out_id);
 dg_status dg_object_destroy(dg_ctx* ctx, int32_t object);
 
+/* ---------------------------------------------------------- OBJ/MTL loader
+ * Object::load_from_file (object.rs:106-454) as a parser whose result the
+ * caller turns into an object with dg_texmap_create and dg_object_create (the
+ * reference decodes texture images with stb_image; this library leaves image
+ * decoding to the caller and returns the map paths). The parser follows the
+ * reference's use of the OBJ data: quads split as (a, b, c), (c, d, a); faces
+ * of more than 4 vertices DG_E_LIMIT (the reference's todo!); normals
+ * normalized; positions scaled so the largest |v| is 100; materials
+ * [Texture::default(), MTL materials in library order]; one mesh per non-empty
+ * group; dummy texture coordinates and generated smooth normals for groups
+ * whose faces lack them. DG_E_INVALID where the reference panics (unopenable
+ * file, missing Ka/Kd/Ks, a face of fewer than 3 vertices, no positions). */
+typedef struct dg_obj dg_obj;
+dg_status dg_obj_parse(const char* path, dg_obj** out);
+/* [0] positions, [1] normals, [2] texture coordinates, [3] meshes, [4] materials, [5] triangles. */
+dg_status dg_obj_counts(const dg_obj* h, uint64_t* out, int32_t n);
+/* Vec3 lists (3 floats each; texture coordinates as (u, v, 0)); any pointer may be NULL. */
+dg_status dg_obj_arrays(const dg_obj* h, float* vertices, float* normals, float* uvs);
+/* Mesh `mesh`: its triangles (9 indices each, as dg_mesh_desc), material index and group name. */
+dg_status dg_obj_mesh(const dg_obj* h, uint64_t mesh, uint32_t* tris, uint64_t cap, uint64_t* ntri,
+                      int32_t* texture_idx, char* name, uint64_t name_cap);
+/* Material i (0 = Texture::default()): constants (map ids set to -1), name and the map file paths
+ * ("" when the material has none). */
+dg_status dg_obj_material(const dg_obj* h, uint64_t i, dg_material* m, char* name, uint64_t name_cap,
+                          char* map_ka, char* map_kd, uint64_t path_cap);
+dg_status dg_obj_name(const dg_obj* h, char* name, uint64_t cap);
+dg_status dg_obj_free(dg_obj* h);
+
 /* -------------------------------------------------------------------- scene */
 /* Scene::new(width, height), scene/mod.rs:760-786: camera at (0,0,150) looking
  * at the origin, light at (0,300,300). */
@@ -167,6 +195,20 @@ dg_status dg_canvas_clear(dg_ctx* ctx, int32_t canvas);                         
  * memory (either pointer may be NULL). Synchronizes; returns kernel errors. */
 dg_status dg_canvas_read(dg_ctx* ctx, int32_t canvas, uint8_t* bgra, float* depth);
 dg_status dg_canvas_write(dg_ctx* ctx, int32_t canvas, const uint8_t* bgra, const float* depth);
+/* Canvas::draw_triangle (canvas.rs:435-575), the GUI's 2D triangles, n of them
+ * drawn in order: verts holds n x 3 vertices of 8 floats (x, y, u, v, r, g, b,
+ * alpha; colour channels integers in 0..255, as Color::Custom), texmap the
+ * texture map whose RGBA texels are blended (-1 = the 1x1 white default map),
+ * clips NULL or n clipping rectangles (x_min, y_min, x_max, y_max). Each covered
+ * pixel blends with the canvas where 0 < depth (the overlay does not write
+ * depth). DG_E_INVALID for a clipping rectangle outside the canvas or a colour
+ * out of range; DG_E_TEXTURE_RANGE as the reference's slice index panics. */
+dg_status dg_canvas_draw_triangles_2d(dg_ctx* ctx, int32_t canvas, const float* verts, uint32_t n, int32_t texmap,
+                                      const uint64_t* clips);
+/* The frame as RGBA bytes (row 0 = top): bytes 0 and 2 of every pixel swapped
+ * and the fourth kept, as Application::export_frame_as prepares it for
+ * stbi_write_png/jpg (app/mod.rs:345-350). Synchronizes; returns kernel errors. */
+dg_status dg_canvas_read_rgba(dg_ctx* ctx, int32_t canvas, uint8_t* rgba);
 /* Device pointers of the canvas buffers (for zero-copy consumers). */
 dg_status dg_canvas_device_ptrs(dg_ctx* ctx, int32_t canvas, void** bgra, void** depth);
 dg_status dg_canvas_size(dg_ctx* ctx, int32_t canvas, uint64_t* width, uint64_t* height);
