@@ -364,6 +364,7 @@ dg_status slot_init(dg_ctx* c, JobSlot& s, cudaStream_t stream) {
 void slot_free(JobSlot& s) {
     if (s.stream) cudaStreamSynchronize(s.stream);
     dfree(s.d_vmask);
+    dfree(s.d_vrec);
     dfree(s.d_vshade);
     dfree(s.d_vmark);
     dfree(s.d_queue);
@@ -450,8 +451,9 @@ uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L
     };
     if (L == 0) L = 1;
     const size_t vmask = cap_after(s.vmask_cap, s.d_vmask, std::max<uint64_t>(V, 1));
+    const size_t vrec = cap_after(s.vrec_cap, s.d_vrec, std::max<uint64_t>(V, 1));
     const size_t vshade = cap_after(s.vshade_cap, s.d_vshade, (V + dg_vrow_extra(T)) * L * 2);
-    const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>((V + 31) / 32, 1));
+    const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>(V, 1));
     const size_t q = cap_after(s.queue_cap, s.d_queue, queue_records(T));
     const size_t sm = cap_after(s.small_cap, s.d_small, queue_records(T));
     const size_t fb = cap_after(s.fb_cap, s.d_fb, P / ((uint64_t)DG_TILE_W * 8u) + 65536u);  // tiles, any tile_rows
@@ -459,7 +461,7 @@ uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L
     const size_t sv = cap_after(s.surv_cap, s.d_surv, std::max<uint64_t>(T, 1));
     const size_t ro = cap_after(s.rec_of_cap, s.d_rec_of, std::max<uint64_t>(T, 1));
     const size_t tr = cap_after(s.trec_cap, s.d_trec, trec_records(T));
-    return vmask * sizeof(uint16_t) + vshade * sizeof(float4) + vmark * sizeof(uint32_t) + (q + sm) * sizeof(DgQueueRec) +
+    return vmask * sizeof(uint16_t) + vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint8_t) + (q + sm) * sizeof(DgQueueRec) +
            qb * sizeof(uint2) + (sv + ro + fb) * sizeof(uint32_t) + tr * sizeof(DgTriRec);
 }
 
@@ -570,6 +572,8 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     if (e) return e;
     e = grow(S, &S.d_vmask, &S.vmask_cap, std::max<uint64_t>(total_vtx, 1));
     if (e) return e;
+    e = grow(S, &S.d_vrec, &S.vrec_cap, std::max<uint64_t>(total_vtx, 1));
+    if (e) return e;
     const uint64_t vrow_extra = dg_vrow_extra(total_tri);
     // rows: job vertices, clip vertices of opaque triangles, 6 per transparent triangle
     e = grow(S, &S.d_vshade, &S.vshade_cap, (total_vtx + vrow_extra + 6 * ntt) * stride * 2);
@@ -620,11 +624,11 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     if (e) return e;
     e = grow(S, &S.d_trec, &S.trec_cap, trec_records(total_tri));
     if (e) return e;
-    const size_t want_mark = std::max<uint64_t>((total_vtx + 31) / 32, 1);
+    const size_t want_mark = std::max<uint64_t>(total_vtx, 1);
     if (S.vmark_cap < want_mark) {
         e = grow(S, &S.d_vmark, &S.vmark_cap, want_mark);
         if (e) return e;
-        DG_CUDA(cudaMemsetAsync(S.d_vmark, 0, S.vmark_cap * sizeof(uint32_t), S.stream));
+        DG_CUDA(cudaMemsetAsync(S.d_vmark, 0, S.vmark_cap * sizeof(uint8_t), S.stream));
     }
     const size_t want_queue = queue_records(total_tri);
     if (S.queue_cap < want_queue) {
@@ -651,6 +655,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.total_tiles = (uint32_t)total_tiles;
     job.shade_stride = stride;
     job.vmask = S.d_vmask;
+    job.vrec = S.d_vrec;
     job.vshade = S.d_vshade;
     job.vrow_extra = (uint32_t)vrow_extra;
     job.vmark = S.d_vmark;

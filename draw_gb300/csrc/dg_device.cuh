@@ -116,15 +116,14 @@ __device__ __forceinline__ float4 vertex_screen(const DgFrameDev& fr, float4 p4,
     return make_float4(cx, cy, depth, __uint_as_float(mask));
 }
 
-// The three vertices of triangle tp of segment sg (vertex_screen of each).
+// The three vertex records (vertex_screen of each, written by k_vertex) of
+// triangle tp of segment sg.
 __device__ __forceinline__ void triangle_vertices(const DgJobDev& job, const DgSegDev& sg, const DgFrameDev& fr,
                                                   uint4 tp, float4 r[3]) {
-    const float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-    const uint16_t* vm = job.vmask + sg.vtx_begin;
-    const uint32_t ma = __ldg(vm + tp.x), mb = __ldg(vm + tp.y), mc = __ldg(vm + tp.z);
-    r[0] = vertex_screen(fr, pa, ma);
-    r[1] = vertex_screen(fr, pb, mb);
-    r[2] = vertex_screen(fr, pc, mc);
+    (void)fr;
+    r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
+    r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
+    r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
 }
 
 // ------------------------------------------------------------ edge set

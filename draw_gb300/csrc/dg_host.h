@@ -113,9 +113,11 @@ struct JobSlot {
     cudaStream_t stream = nullptr;
     uint16_t* d_vmask = nullptr;  // plane-sign masks of the job's vertices
     size_t vmask_cap = 0;
+    float4* d_vrec = nullptr;  // vertex records (screen centre, eye distance, masks)
+    size_t vrec_cap = 0;
     float4* d_vshade = nullptr;
     size_t vshade_cap = 0;
-    uint32_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
+    uint8_t* d_vmark = nullptr;  // zeroed at allocation; the queue pass clears what setup sets
     size_t vmark_cap = 0;
     DgQueueRec* d_queue = nullptr;
     DgQueueRec* d_small = nullptr;  // small-triangle list

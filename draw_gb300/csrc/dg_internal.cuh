@@ -9,8 +9,9 @@
 //   canvas        : colour u32[W*H] (BGRA bytes, row 0 = top), depth f32[W*H]
 //                   (y*W+x, y = 0 at the bottom), vis u64[W*H] (visibility keys,
 //                   kept at DG_VIS_EMPTY between frames)
-//   render scratch: vmask u16[V_total] (plane-sign masks of each vertex),
-//                   vshade float4[V_total*L*2] (light, halfway),
+//   render scratch: vrec float4[V_total] (snapped centre x,y, eye distance,
+//                   plane-sign masks), vmask u16[V_total] (the masks alone, for
+//                   the cull's gathers), vshade float4[V_total*L*2] (light, halfway),
 //                   raster-queue records + their work-unit bases, counters
 #pragma once
 
@@ -181,10 +182,11 @@ struct DgJobDev {
     uint32_t nframes, nsegs;
     uint32_t total_vtx, total_tri, total_tiles;
     uint32_t shade_stride;  // lights per row of vshade (max over frames)
+    float4* vrec;           // [total_vtx] snapped screen centre, eye distance, plane-sign mask bits
     uint16_t* vmask;        // [total_vtx] bit p: plane p has f > 0; bit 8 + p: f <= 0 (near, far, 4 lateral)
     float4* vshade;         // rows [0, total_vtx): job vertices; then rows for clip vertices
     uint32_t vrow_extra;    // rows after total_vtx available to clip vertices
-    uint32_t* vmark;        // one bit per job vertex: needs light/halfway vectors (kept zero between jobs)
+    uint8_t* vmark;         // one byte per job vertex: needs light/halfway vectors (kept zero between jobs)
     uint32_t* surv;         // [total_tri] job-wide indices of the triangles that passed the cull pass
     uint32_t* rec_of;       // [total_tri] first DgTriRec of each surviving triangle, or DG_NONE
     DgTriRec* trec;

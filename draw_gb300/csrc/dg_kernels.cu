@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
             if (f > 0.0f) mask |= 1u << pl;
             if (f <= 0.0f) mask |= 1u << (8 + pl);
         }
+        job.vrec[v] = vertex_screen(fr, p4, mask);
         job.vmask[v] = (uint16_t)mask;
     }
 }
@@ -63,11 +64,14 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
 // set; the plane tests read only the vertex records' sign masks. Survivors are
 // appended (in any order: the visibility key carries the submission index).
 __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
+    __shared__ uint32_t s_warp[8];
+    __shared__ unsigned long long s_base;
     wait_previous_kernel();
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < job.total_tri; base += stride) {
-        const uint32_t g = base + lane;
+    // block-uniform loop: survivors are appended with one atomic per block
+    for (uint32_t base = blockIdx.x * blockDim.x; base < job.total_tri; base += stride) {
+        const uint32_t g = base + threadIdx.x;
         bool keep = false;
         if (g < job.total_tri) {
             const uint32_t si = seg_of_tri(job, g);
@@ -88,13 +92,20 @@ __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
             }
         }
         const unsigned kb = __ballot_sync(FULL, keep);
-        if (kb) {
-            const int leader = __ffs(kb) - 1;
-            unsigned long long old = 0;
-            if ((int)lane == leader) old = atomicAdd(job.cnt + DG_CNT_SURV, (unsigned long long)__popc(kb));
-            old = __shfl_sync(FULL, old, leader);
-            if (keep) job.surv[old + __popc(kb & ((1u << lane) - 1u))] = g;
+        if (lane == 0u) s_warp[wid] = (uint32_t)__popc(kb);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (uint32_t w = 0; w < 8u; w++) {
+                const uint32_t c = s_warp[w];
+                s_warp[w] = run;
+                run += c;
+            }
+            s_base = run ? atomicAdd(job.cnt + DG_CNT_SURV, (unsigned long long)run) : 0ull;
         }
+        __syncthreads();
+        if (keep) job.surv[s_base + s_warp[wid] + __popc(kb & ((1u << lane) - 1u))] = g;
+        __syncthreads();  // s_warp and s_base are reused by the next iteration
     }
 }
 
@@ -103,7 +114,29 @@ __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
 // clipping, triangle records, bounding boxes and edge functions; tiny
 // triangles are rasterized by their warp, the others are queued
 // (scene/mod.rs:1029-1063, canvas.rs:585-681).
+// Hands out n consecutive slots of counter c to every lane of the (converged)
+// warp with one atomic; returns this lane's first slot.
+__device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* c, uint32_t n) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    unsigned long long old = 0;
+    if (total != 0u) {
+        if (lane == 31u) old = atomicAdd(c, (unsigned long long)total);
+        old = __shfl_sync(FULL, old, 31);
+    }
+    return old + (incl - n);
+}
+
 __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
+    __shared__ uint32_t s_records;  // statistics: record requests of the block
+    if (threadIdx.x == 0) s_records = 0u;
+    __syncthreads();
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long ns64 = __ldcg(job.cnt + DG_CNT_SURV);
@@ -116,6 +149,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
         uint4 tp = make_uint4(0, 0, 0, 0), tuv = tp, tnr = tp;
         float4 r[3];
         bool clipped = false;
+        ClipProg P;  // built once per clipped triangle, used by every output
         if (i < nsurv) {
             g = __ldcg(job.surv + i);
             si = seg_of_tri(job, g);
@@ -131,40 +165,45 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             } else {
                 const DgFrameDev& fr = job.frames[sg.frame];
                 float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-                ClipProg P;
                 build_clip(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z}, P);
                 nout = P.nout;
                 clipped = true;
-                if (nout > 0 && P.nv > 3) {
-                    // rows of the light/halfway table for the new vertices
-                    nrows = (uint32_t)(P.nv - 3);
-                    const unsigned long long r0 = atomicAdd(job.cnt + DG_CNT_VROW, (unsigned long long)nrows);
-                    if (r0 + nrows <= job.vrow_extra) {
-                        row0 = (uint32_t)r0;
-                        clip_shade_rows(job, fr, P, job.total_vtx + row0);
-                    } else {
-                        nrows = DG_NONE;  // no room: the resolve pass shades these pixels the long way
-                    }
-                }
+                if (nout > 0 && P.nv > 3) nrows = (uint32_t)(P.nv - 3);  // light rows for the new vertices
             }
             if (nout > 0) {  // its vertices need light/halfway vectors for shading
                 const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
-                for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+                for (int k = 0; k < 3; k++) job.vmark[vv[k]] = 1u;  // plain stores: every writer writes 1
+            }
+        }
+        // Rows of the light/halfway table for clip vertices, one atomic per warp.
+        {
+            const unsigned long long r0 = warp_alloc(job.cnt + DG_CNT_VROW, nrows);
+            if (nrows != 0u) {
+                if (r0 + nrows <= job.vrow_extra) {
+                    row0 = (uint32_t)r0;
+                    clip_shade_rows(job, job.frames[job.segs[si].frame], P, job.total_vtx + row0);
+                } else {
+                    nrows = DG_NONE;  // no room: the fallback pass shades these pixels the long way
+                }
             }
         }
         // Triangle records: a triangle with one output uses record i (its survivor
         // slot); the clip outputs of one with more take consecutive records after
-        // the first total_tri.
+        // the first total_tri (one atomic per warp).
         uint32_t rbase = DG_NONE;
-        if (nout == 1 && nrows != DG_NONE) {
-            if (i < job.trec_cap) rbase = i;
-        } else if (nout > 1 && nrows != DG_NONE) {
-            const unsigned long long rb =
-                (unsigned long long)job.total_tri + atomicAdd(job.cnt + DG_CNT_TRECX, (unsigned long long)nout);
-            if (rb + (unsigned long long)nout <= job.trec_cap) rbase = (uint32_t)rb;
+        {
+            const uint32_t multi = (nout > 1 && nrows != DG_NONE) ? (uint32_t)nout : 0u;
+            const unsigned long long rb = (unsigned long long)job.total_tri + warp_alloc(job.cnt + DG_CNT_TRECX, multi);
+            if (nout == 1 && nrows != DG_NONE) {
+                if (i < job.trec_cap) rbase = i;
+            } else if (multi && rb + (unsigned long long)nout <= job.trec_cap) {
+                rbase = (uint32_t)rb;
+            }
         }
-        const uint32_t nrec = __reduce_add_sync(FULL, (uint32_t)nout);
-        if (lane == 0u && nrec) atomicAdd(job.cnt + DG_CNT_TREC, (unsigned long long)nrec);  // statistics only
+        {
+            const uint32_t nrec = __reduce_add_sync(FULL, (uint32_t)nout);
+            if (lane == 0u && nrec) atomicAdd(&s_records, nrec);  // 32-bit shared atomic, one per warp
+        }
         if (i < nsurv) job.rec_of[g] = rbase;
 
         for (int rr = 0;; rr++) {
@@ -183,15 +222,12 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                 const DgFrameDev& fr = job.frames[sg.frame];
                 tr.frame = sg.frame;
                 tr.seq = ((sg.seq_base + t) << 2) | (uint32_t)rr;
-                ClipProg P;
                 if (!clipped) {
                     tr.ax = r[0].x; tr.ay = r[0].y;
                     tr.bx = r[1].x; tr.by = r[1].y;
                     tr.cx = r[2].x; tr.cy = r[2].y;
                     tr.da = r[0].z; tr.db = r[1].z; tr.dc = r[2].z;
                 } else {
-                    float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-                    build_clip(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z}, P);
                     clip_output_tri(fr, P, rr, r, tr);
                 }
                 bool nan = isnan(tr.ax) || isnan(tr.ay) || isnan(tr.bx) || isnan(tr.by) || isnan(tr.cx) ||
@@ -325,6 +361,8 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
             }
         }
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_records) atomicAdd(job.cnt + DG_CNT_TREC, (unsigned long long)s_records);  // statistics only
 }
 
 // The raster queue: the bounding-box pixels of every queued triangle in
@@ -361,14 +399,15 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
     uint32_t* by = s_by[threadIdx.x >> 5];
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    // Prologue: light/halfway vectors of the vertices the setup pass marked, one
-    // mark word (32 vertices) per warp; the words are cleared for the next job.
-    const uint32_t nwords = (job.total_vtx + 31u) >> 5;
-    for (uint32_t w = warp; w < nwords; w += nwarps) {
-        const uint32_t bits = __ldcg(job.vmark + w);
-        if (bits == 0u) continue;
-        if (((bits >> lane) & 1u) && (w << 5) + lane < job.total_vtx) shade_vertex(job, (w << 5) + lane);
-        if (lane == 0) job.vmark[w] = 0u;
+    // Prologue: light/halfway vectors of the vertices the setup pass marked, 32
+    // vertices per warp; the marks are cleared for the next job.
+    const uint32_t ngroups = (job.total_vtx + 31u) >> 5;
+    for (uint32_t w = warp; w < ngroups; w += nwarps) {
+        const uint32_t v = (w << 5) + lane;
+        if (v < job.total_vtx && __ldcg(job.vmark + v)) {
+            shade_vertex(job, v);
+            job.vmark[v] = 0u;
+        }
     }
     const unsigned long long cnt = __ldcg(job.cnt + DG_CNT_QUEUE);
     const uint64_t ni64 = cnt & ((1ull << DG_PACK_SHIFT) - 1ull);

@@ -33,10 +33,11 @@ constexpr size_t kOffDesc = 0;
 constexpr uint32_t kVrowExtra = 4096;  // light/halfway rows for clip vertices
 constexpr uint32_t kTrecCap = (uint32_t)dg_trec_cap(DG_NOALLOC_MAX_TRIANGLES);  // triangle records
 constexpr size_t kOffVrec = align_up(kOffDesc + sizeof(NoallocDesc));
-constexpr size_t kOffVshade = align_up(kOffVrec + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(uint16_t));
+constexpr size_t kOffVmask = align_up(kOffVrec + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(float4));
+constexpr size_t kOffVshade = align_up(kOffVmask + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(uint16_t));
 constexpr size_t kOffVmark = align_up(kOffVshade + (size_t)(DG_NOALLOC_MAX_VERTICES + kVrowExtra) *
                                                        DG_NOALLOC_MAX_LIGHTS * 2 * sizeof(float4));
-constexpr size_t kOffQueue = align_up(kOffVmark + (size_t)(DG_NOALLOC_MAX_VERTICES / 32) * sizeof(uint32_t));
+constexpr size_t kOffQueue = align_up(kOffVmark + (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(uint8_t));
 constexpr size_t kOffSmall = align_up(kOffQueue + (size_t)kQueueCap * sizeof(DgQueueRec));
 constexpr size_t kOffQbase = align_up(kOffSmall + (size_t)kQueueCap * sizeof(DgQueueRec));
 constexpr size_t kOffSurv = align_up(kOffQbase + (size_t)dg_items_cap(kQueueCap) * sizeof(uint2));
@@ -201,10 +202,11 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.total_tiles = tiles;
     job.fb_tiles = reinterpret_cast<uint32_t*>(base + kOffFb);
     job.shade_stride = p->nlights;
-    job.vmask = reinterpret_cast<uint16_t*>(base + kOffVrec);
+    job.vrec = reinterpret_cast<float4*>(base + kOffVrec);
+    job.vmask = reinterpret_cast<uint16_t*>(base + kOffVmask);
     job.vshade = reinterpret_cast<float4*>(base + kOffVshade);
     job.vrow_extra = kVrowExtra;
-    job.vmark = reinterpret_cast<uint32_t*>(base + kOffVmark);
+    job.vmark = reinterpret_cast<uint8_t*>(base + kOffVmark);
     job.surv = reinterpret_cast<uint32_t*>(base + kOffSurv);
     job.rec_of = reinterpret_cast<uint32_t*>(base + kOffRecOf);
     job.trec = reinterpret_cast<DgTriRec*>(base + kOffTrec);
@@ -233,7 +235,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     // Reset what the previous call left behind.
     NA_CUDA(cudaMemsetAsync(base + kOffCounters, 0, DG_NCOUNTERS * sizeof(unsigned long long), s));
     NA_CUDA(cudaMemsetAsync(base + kOffErr, 0, sizeof(uint32_t), s));
-    NA_CUDA(cudaMemsetAsync(base + kOffVmark, 0, (size_t)(DG_NOALLOC_MAX_VERTICES / 32) * sizeof(uint32_t), s));
+    NA_CUDA(cudaMemsetAsync(base + kOffVmark, 0, (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(uint8_t), s));
     NA_CUDA(cudaMemsetAsync(base + kOffWhite, 0xFF, 8, s));
     NA_CUDA(dg_launch_vis_reset(reinterpret_cast<uint64_t*>(base + kOffVis), npx, s));
 

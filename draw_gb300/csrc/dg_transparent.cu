@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(256) k_tsetup(const DgJobDev job) {
         }
         if (nout > 0) {  // its vertices need light/halfway vectors for shading
             const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
-            for (int k = 0; k < 3; k++) atomicOr(job.vmark + (vv[k] >> 5), 1u << (vv[k] & 31u));
+            for (int k = 0; k < 3; k++) job.vmark[vv[k]] = 1u;
         }
         const float alpha = tp.w < sg.nmats ? __ldg(&sg.mats[tp.w].alpha) : 1.0f;
         const uint32_t tseq = (j - fr.tt_begin) << 2;

@@ -107,7 +107,7 @@ dg_status dg_ctx_get_tuning(dg_ctx* ctx, dg_tuning* t);
  * pixels (written by resolve), [5] triangles rasterized in place because the queue, the
  * small-triangle list or the triangle records were full, [6] host-to-device bytes of the
  * job descriptor, [7] kernels launched, [8] triangles that passed the cull pass,
- * [9] triangle records handed out, [10] light/halfway rows handed out to clip vertices,
+ * [9] triangles (clip outputs counted one by one) that asked for a triangle record, [10] light/halfway rows handed out to clip vertices,
  * [11] triangles on the small-triangle list. Synchronizes. */
 dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
 
