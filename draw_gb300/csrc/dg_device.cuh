@@ -24,6 +24,24 @@ __device__ __forceinline__ float fS(float a, float b) { return __fsub_rn(a, b); 
 __device__ __forceinline__ float fM(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fD(float a, float b) { return __fdiv_rn(a, b); }
 
+// a / b rounded to nearest from y = RN(1/b), by Markstein's method (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000 processor",
+// IBM J. Res. Develop. 34(1), 1990): q0 = RN(a*y) is within two ulps of a/b; one
+// residual step q1 = RN(q0 + RN(a - b*q0)*y) makes it faithful, after which the
+// residual a - b*q1 is exact (an FMA) and RN(q1 + (a - b*q1)*y) is RN(a/b).
+// Callers guarantee the steps neither overflow nor underflow: b integer-valued
+// in [1, 2^100), a integer-valued with |a| < 2^100, so a nonzero quotient is at
+// least 2^-100 and every nonzero residual at least 2^-123. A zero a returns a*y,
+// which is the zero of the same sign that a / b gives.
+__device__ __forceinline__ float div_rcp(float a, float b, float y) {
+    const float q0 = __fmul_rn(a, y);
+    const float r0 = __fmaf_rn(-q0, b, a);
+    const float q1 = __fmaf_rn(r0, y, q0);
+    const float r1 = __fmaf_rn(-q1, b, a);
+    const float q2 = __fmaf_rn(r1, y, q1);
+    return a == 0.0f ? q0 : q2;
+}
+
 struct V3 {
     float x, y, z;
 };
@@ -170,6 +188,19 @@ __device__ __forceinline__ void make_edges(float ax, float ay, float bx, float b
         fast = fast && e.den[k] > 0.0f && e.den[k] < INFINITY;
     }
     if (fast) e.tie |= DG_EDGE_FAST;
+}
+
+// Whether the barycentric divisions of an edge set may use div_rcp: every den
+// is finite, > 0 and below 2^100 (DG_EDGE_FAST makes them integer-valued and so
+// >= 1), |A|, |B| < 2^64 and |C|, |D| < 2^98, so that the edge value at any
+// pixel (coordinates below 2^32) stays below 2^100 in magnitude.
+__device__ __forceinline__ bool edge_rcp_ok(const EdgeSet& e) {
+    bool ok = (e.tie & DG_EDGE_FAST) != 0u;
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        ok = ok && e.den[k] < 0x1p100f && fabsf(e.A[k]) < 0x1p64f && fabsf(e.B[k]) < 0x1p64f &&
+             fabsf(e.C[k]) < 0x1p98f && fabsf(e.D[k]) < 0x1p98f;
+    return ok;
 }
 
 // Division-free early reject, exact with respect to the reference's test.
@@ -542,7 +573,17 @@ __device__ __noinline__ void write_clip_record(const DgJobDev& job, DgTriRec* R,
 // Kernels launched with programmatic dependent launch start before the previous
 // kernel of the stream has finished; this waits until it has completed and its
 // memory operations are visible.
-__device__ __forceinline__ void wait_previous_kernel() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel of the stream (one launched by launch_dependent) be
+// scheduled as soon as every block of this grid has started. That kernel still
+// waits in wait_previous_kernel() until this grid has completed and its writes
+// are visible, so the early start only overlaps its launch and prologue.
+__device__ __forceinline__ void allow_next_kernel() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// Waits until the previous kernel of the stream has completed and its writes are
+// visible (a no-op after a plain launch); lets the next kernel be scheduled first.
+__device__ __forceinline__ void wait_previous_kernel() {
+    allow_next_kernel();
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 
 // Rasterizes a triangle's clipped bounding box on the calling lane alone, row
 // by row (the pixel position advances without division).

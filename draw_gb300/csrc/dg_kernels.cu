@@ -35,6 +35,7 @@ namespace {
 
 // ================================================================ kernels
 __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
+    allow_next_kernel();
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < job.total_vtx; v += stride) {
         uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
@@ -371,13 +372,21 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
 // One candidate fragment of a queued triangle (its pixel passed prereject):
 // the coverage test with the divisions, the depth, the strict test against the
 // clear depth and the keyed minimum.
+// rcp (uniform over the warp): the edge set passed edge_rcp_ok and yr holds the
+// reciprocals of its three dens.
 __device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uint32_t seq, uint32_t x, uint32_t y,
-                                                float clear_depth, unsigned long long* vis, uint32_t width) {
+                                                float clear_depth, unsigned long long* vis, uint32_t width, bool rcp,
+                                                float3 yr) {
     float al, be, ga;
     const float xf = (float)x, yf = (float)y;
     const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
     bool cov;
-    if (e.tie & DG_EDGE_FAST) {  // the candidate passed the sign test: only the barycentrics remain
+    if (rcp) {  // the candidate passed the sign test: only the barycentrics remain
+        al = div_rcp(n0, e.den[0], yr.x);
+        be = div_rcp(n1, e.den[1], yr.y);
+        ga = div_rcp(n2, e.den[2], yr.z);
+        cov = true;
+    } else if (e.tie & DG_EDGE_FAST) {
         al = fD(n0, e.den[0]);
         be = fD(n1, e.den[1]);
         ga = fD(n2, e.den[2]);
@@ -391,7 +400,7 @@ __device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uin
     }
 }
 
-__global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
+__global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
     __shared__ uint32_t s_bx[8][64], s_by[8][64];  // per-warp candidate buffers
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
@@ -445,7 +454,6 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
         unsigned long long* vis = reinterpret_cast<unsigned long long*>(fr.vis);
         const uint32_t width = fr.width;
         const uint32_t xlo = q0.w, ylo = q1.x, w = q1.y, npx = q1.z;
-        const float rcp_w = __frcp_rn((float)w);
         const uint32_t u_end = min(q1.w, item.y + job.item_units);
         // Stage A: every lane takes one pixel of the unit and applies the exact,
         // division-free pre-reject; candidates are packed into the warp's buffer.
@@ -454,22 +462,25 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
         // depth key), so the division path runs with all lanes busy.
         uint32_t pending = 0;
         const bool fast = (e.tie & DG_EDGE_FAST) != 0u;
-        for (uint32_t u = item.y; u < u_end; u++) {
-            // the unit's first pixel: k0 / w from a float reciprocal, corrected to the exact quotient
-            const uint32_t k0 = u * DG_UNIT_PX;
-            uint32_t y0 = (uint32_t)__fmul_rz((float)k0, rcp_w);
-            while ((uint64_t)y0 * w > k0) y0--;
-            while ((uint64_t)(y0 + 1u) * w <= k0) y0++;
-            // this lane's pixel, k0 + lane, by stepping along the rows
-            uint32_t xx = (k0 - y0 * w) + lane, yy = y0;
-            if (xx >= w) {
-                const uint32_t q = w >= DG_UNIT_PX ? 1u : xx / w;
-                xx -= q * w;
-                yy += q;
-            }
+        const bool rcp = edge_rcp_ok(e);
+        const float3 yr = rcp ? make_float3(__frcp_rn(e.den[0]), __frcp_rn(e.den[1]), __frcp_rn(e.den[2]))
+                              : make_float3(0.0f, 0.0f, 0.0f);
+        // This lane's pixel k = u * DG_UNIT_PX + lane of the box, as column xx and
+        // row yy: one division per item, then a step of DG_UNIT_PX pixels per unit
+        // (q32 rows and r32 columns, with at most one carry since xx, r32 < w).
+        uint32_t k = item.y * DG_UNIT_PX + lane;
+        uint32_t yy = k / w, xx = k - yy * w;
+        const uint32_t q32 = DG_UNIT_PX / w, r32 = DG_UNIT_PX - q32 * w;
+        for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
             bool cand = false;
             const uint32_t x = xlo + xx, y = ylo + yy;
-            if (k0 + lane < npx) {
+            xx += r32;
+            yy += q32;
+            if (xx >= w) {
+                xx -= w;
+                yy++;
+            }
+            if (k < npx) {
                 const float xf = (float)x, yf = (float)y;
                 const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
                 cand = fast ? covered_signs(e.tie, n0, n1, n2)
@@ -484,7 +495,7 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
             pending += __popc(b);
             if (pending >= 32u) {
                 __syncwarp();
-                finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width);
+                finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);
                 __syncwarp();
                 if (lane < pending - 32u) {
                     bx[lane] = bx[32u + lane];
@@ -495,7 +506,7 @@ __global__ void __launch_bounds__(256) k_queue_raster(const DgJobDev job) {
             }
         }
         __syncwarp();
-        if (lane < pending) finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width);
+        if (lane < pending) finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);
         __syncwarp();
     }
 }
