@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
 SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu", "dg_transparent.cu",
-           "dg_loader.cpp"]
+           "dg_selfcheck.cu", "dg_loader.cpp"]
 HEADERS = ["dg_internal.cuh", "dg_host.h", "dg_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

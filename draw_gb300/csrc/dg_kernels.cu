@@ -529,7 +529,7 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
     __shared__ DgTexDev stex[DG_SMEM_TEX];
     __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
     __shared__ uint32_t s_val[DG_TILE_W * TH];  // triangle record
-    __shared__ uint32_t s_row[34];  // shade-list offset of each tile row; [32] = total, [33] = pixels without record
+    __shared__ uint32_t s_row[33];  // shade-list offset of each tile row; [32] = total
     // independent of the previous kernel: the quotient table and the texture descriptors
     inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
     const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
@@ -537,7 +537,6 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
         reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_row[33] = 0u;
     const uint32_t tile = blockIdx.x;
     const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
     const DgFrameDev& fr = job.frames[fi];
@@ -555,6 +554,7 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
     }
     uint32_t val[R];
     unsigned hit[R];
+    int no_record = 0;
 #pragma unroll
     for (int j = 0; j < R; j++) {
         const uint32_t y = ty * TH + wid + 8u * j;
@@ -580,13 +580,13 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
                 fr.vis[i] = DG_VIS_EMPTY;
             } else {
                 val[j] = DG_NONE;  // shaded by the fallback pass, which resets the key
-                s_row[33] = 1u;
+                no_record = 1;
             }
         }
         hit[j] = __ballot_sync(FULL, covered_px && val[j] != DG_NONE);
         if (lane == 0) s_row[wid + 8u * j] = __popc(hit[j]);
     }
-    __syncthreads();
+    const int any_no_record = __syncthreads_or(no_record);
     if (wid == 0) {  // exclusive scan of the TH row counts
         const uint32_t c = lane < TH ? s_row[lane] : 0u;
         uint32_t incl = c;
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
         fr.colour[(uint64_t)(H - 1u - py) * W + px] = c;
     }
     // a tile with pixels whose triangle has no record goes to the fallback pass
-    if (threadIdx.x == 0 && s_row[33] != 0u) {
+    if (threadIdx.x == 0 && any_no_record) {
         const unsigned long long slot = atomicAdd(job.cnt + DG_CNT_FBTILES, 1ull);
         if (slot < job.total_tiles) job.fb_tiles[slot] = tile;
     }

@@ -38,6 +38,7 @@ SIGNATURES = {
     "dg_ctx_set_timing": (_i32, [_P, _i32]),
     "dg_ctx_kernel_times": (_i32, [_P, _P, _i32]),
     "dg_ctx_last_stats": (_i32, [_P, _P, _i32]),
+    "dg_check_division": (_i32, [_P, _i32, _u64, _u64, _P, _P, _P]),
     "dg_ctx_set_tuning": (_i32, [_P, _P]),
     "dg_ctx_get_tuning": (_i32, [_P, _P]),
     "dg_texmap_create": (_i32, [_P, _P, _u64, _u64, _u64, _u64, _P]),
@@ -231,6 +232,13 @@ class Context:
         v = (ctypes.c_uint64 * len(STATS_KEYS))()
         _chk(self.lib.dg_ctx_last_stats(self.h, v, len(STATS_KEYS)), "last_stats")
         return dict(zip(STATS_KEYS, list(v)))
+
+    def check_division(self, mode: int, samples: int, seed: int = 1) -> tuple:
+        """dg_check_division: (mismatches, first mismatching a, b) of one sample family."""
+        n, a, b = ctypes.c_uint64(), ctypes.c_float(), ctypes.c_float()
+        _chk(self.lib.dg_check_division(self.h, mode, samples, seed, ctypes.byref(n), ctypes.byref(a),
+                                        ctypes.byref(b)), "check_division")
+        return n.value, a.value, b.value
 
     def render_batch(self, scenes: list, canvases: list):
         """The batched form: all frames in one launch per pipeline stage."""

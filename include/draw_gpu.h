@@ -111,6 +111,17 @@ dg_status dg_ctx_get_tuning(dg_ctx* ctx, dg_tuning* t);
  * [11] triangles on the small-triangle list. Synchronizes. */
 dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
 
+/* Self-check of the division the raster pass uses for the barycentrics of a
+ * covered pixel: a / b computed from the reciprocal RN(1/b) by two residual
+ * corrections (Markstein's method) must equal IEEE a / b bit for bit. Checks
+ * `samples` seeded pairs (a, b) and (-a, b) of one family on the device:
+ * mode 0 every integer pair 0 <= a <= b <= 4096, mode 1 integers b <= 2^24 and
+ * a <= b, mode 2 integer-valued b < 2^101 and a < 4b, mode 3 a < 2^61 and
+ * b < 2^100 with random mantissas. Writes the mismatch count and, when there is
+ * one, the first mismatching pair seen. Synchronizes. */
+dg_status dg_check_division(dg_ctx* ctx, int32_t mode, uint64_t samples, uint64_t seed, uint64_t* mismatches,
+                            float* first_a, float* first_b);
+
 /* -------------------------------------------------------------- texture map */
 /* TextureMap::new(img, width, height, components), scene/mod.rs:113-126. */
 dg_status dg_texmap_create(dg_ctx* ctx, const uint8_t* img, uint64_t len, uint64_t width, uint64_t height,
