@@ -282,9 +282,23 @@ Scene* get_scene(dg_ctx* c, int32_t id) {
     if (!c || id < 0 || (size_t)id >= c->scenes.size()) return nullptr;
     return &c->scenes[id];
 }
+// Every operation on a canvas looks it up here, so a pending asynchronous read
+// is ordered before whatever the context stream does to the canvas next.
 Canvas* get_canvas(dg_ctx* c, int32_t id) {
     if (!c || id < 0 || (size_t)id >= c->canvases.size() || !c->canvases[id].alive) return nullptr;
-    return &c->canvases[id];
+    Canvas* v = &c->canvases[id];
+    if (v->read_pending) {
+        cudaStreamWaitEvent(c->main.stream, v->ev_read, 0);
+        v->read_pending = false;
+    }
+    return v;
+}
+void free_canvas(Canvas& v) {
+    dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
+    if (v.ev_rendered) cudaEventDestroy(v.ev_rendered);
+    if (v.ev_read) cudaEventDestroy(v.ev_read);
+    v.ev_rendered = v.ev_read = nullptr;
+    v.read_pending = false;
 }
 Object* get_object(dg_ctx* c, int32_t id) {
     if (!c || id < 0 || (size_t)id >= c->objects.size() || !c->objects[id].alive) return nullptr;
@@ -855,9 +869,8 @@ dg_status dg_ctx_destroy(dg_ctx* c) {
     cudaDeviceSynchronize();
     for (auto& t : c->tex) dfree(t.d_words);
     for (auto& o : c->objects) free_object(o);
-    for (auto& v : c->canvases) {
-        dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
-    }
+    for (auto& v : c->canvases) free_canvas(v);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     dfree(c->d_tex);
     slot_free(c->main);
     {
@@ -1209,7 +1222,7 @@ dg_status dg_canvas_destroy(dg_ctx* c, int32_t id) {
     if (!v) return DG_E_INVALID;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->main.stream);
-    dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis);
+    free_canvas(*v);
     v->alive = false;
     return DG_OK;
 }
@@ -1287,6 +1300,43 @@ dg_status dg_canvas_read(dg_ctx* c, int32_t id, uint8_t* bgra, float* depth) {
     if (depth) DG_CUDA(cudaMemcpyAsync(depth, v->d_depth, n * 4, cudaMemcpyDeviceToHost, st));
     DG_CUDA(cudaStreamSynchronize(st));
     return slot_take_errors(c->main);
+}
+
+dg_status dg_canvas_read_async(dg_ctx* c, int32_t id, uint8_t* bgra, float* depth) {
+    Canvas* v = get_canvas(c, id);
+    if (!v) return DG_E_INVALID;
+    if (depth && !v->depth_init) return DG_E_DEPTH_UNINIT;
+    dg_status e = set_device(c);
+    if (e) return e;
+    if (!c->copy_stream) DG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    if (!v->ev_rendered) DG_CUDA(cudaEventCreateWithFlags(&v->ev_rendered, cudaEventDisableTiming));
+    if (!v->ev_read) DG_CUDA(cudaEventCreateWithFlags(&v->ev_read, cudaEventDisableTiming));
+    const uint64_t n = v->w * v->h;
+    DG_CUDA(cudaEventRecord(v->ev_rendered, c->main.stream));
+    DG_CUDA(cudaStreamWaitEvent(c->copy_stream, v->ev_rendered, 0));
+    if (bgra) DG_CUDA(cudaMemcpyAsync(bgra, v->d_colour, n * 4, cudaMemcpyDeviceToHost, c->copy_stream));
+    if (depth) DG_CUDA(cudaMemcpyAsync(depth, v->d_depth, n * 4, cudaMemcpyDeviceToHost, c->copy_stream));
+    DG_CUDA(cudaEventRecord(v->ev_read, c->copy_stream));
+    v->read_pending = true;
+    return DG_OK;
+}
+
+dg_status dg_canvas_read_wait(dg_ctx* c, int32_t id) {
+    if (!c || id < 0 || (size_t)id >= c->canvases.size() || !c->canvases[id].alive) return DG_E_INVALID;
+    Canvas* v = &c->canvases[id];
+    dg_status e = set_device(c);
+    if (e) return e;
+    if (!v->ev_read) return DG_OK;  // never read asynchronously
+    DG_CUDA(cudaEventSynchronize(v->ev_read));
+    // the frames before the copy have completed; their error word is read without
+    // clearing it (later frames may still be running), so the next synchronous
+    // call reports it again
+    uint32_t err = 0;
+    DG_CUDA(cudaMemcpyAsync(&err, c->main.d_err, 4, cudaMemcpyDeviceToHost, c->copy_stream));
+    DG_CUDA(cudaStreamSynchronize(c->copy_stream));
+    for (int b = 1; b < 32; b++)
+        if (err & (1u << b)) return (dg_status)b;
+    return DG_OK;
 }
 
 dg_status dg_canvas_write(dg_ctx* c, int32_t id, const uint8_t* bgra, const float* depth) {

@@ -95,6 +95,11 @@ struct Canvas {
     bool depth_init = false;
     float depth_max = 0.0f;
     float off_x = 0.0f, off_y = 0.0f;
+    // dg_canvas_read_async: the copy runs on the context's copy stream after
+    // ev_rendered; ev_read marks its end. While read_pending, the next operation
+    // that looks the canvas up first makes the context stream wait for ev_read.
+    cudaEvent_t ev_rendered = nullptr, ev_read = nullptr;
+    bool read_pending = false;
 };
 
 // The buffers one frame renders into.
@@ -198,6 +203,7 @@ struct dg_ctx {
     int device = 0;
     int nsm = 152;
     cudaStream_t own_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;  // device-to-host copies of dg_canvas_read_async
     std::vector<dgh::TexMap> tex;  // [0] = 1x1 white default map
     DgTexDev* d_tex = nullptr;
     size_t d_tex_cap = 0;

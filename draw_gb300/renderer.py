@@ -60,6 +60,8 @@ SIGNATURES = {
     "dg_canvas_resize": (_i32, [_P, _i32, _u64, _u64]),
     "dg_canvas_clear": (_i32, [_P, _i32]),
     "dg_canvas_read": (_i32, [_P, _i32, _P, _P]),
+    "dg_canvas_read_async": (_i32, [_P, _i32, _P, _P]),
+    "dg_canvas_read_wait": (_i32, [_P, _i32]),
     "dg_canvas_write": (_i32, [_P, _i32, _P, _P]),
     "dg_canvas_device_ptrs": (_i32, [_P, _i32, _P, _P]),
     "dg_canvas_size": (_i32, [_P, _i32, _P, _P]),
@@ -628,6 +630,14 @@ class Canvas:
 
     def read_into(self, bgra: np.ndarray, depth: np.ndarray | None):
         _chk(self.ctx.lib.dg_canvas_read(self.ctx.h, self.id, _ptr(bgra), _ptr(depth)), "Canvas::read")
+
+    def read_async(self, bgra: np.ndarray | None, depth: np.ndarray | None = None):
+        """dg_canvas_read_async: starts the copy into the (pinned) host arrays and
+        returns; the arrays are valid after read_wait()."""
+        _chk(self.ctx.lib.dg_canvas_read_async(self.ctx.h, self.id, _ptr(bgra), _ptr(depth)), "Canvas::read_async")
+
+    def read_wait(self):
+        _chk(self.ctx.lib.dg_canvas_read_wait(self.ctx.h, self.id), "Canvas::read_wait")
 
     def write(self, bgra: np.ndarray | None, depth: np.ndarray | None):
         b = None if bgra is None else np.ascontiguousarray(bgra, np.uint8)

@@ -205,6 +205,16 @@ dg_status dg_canvas_clear(dg_ctx* ctx, int32_t canvas);                         
 /* Canvas::as_bytes_slice (canvas.rs:974-978) and the depth buffer, copied to host
  * memory (either pointer may be NULL). Synchronizes; returns kernel errors. */
 dg_status dg_canvas_read(dg_ctx* ctx, int32_t canvas, uint8_t* bgra, float* depth);
+/* The same copy without waiting: it starts once the work already queued on the
+ * context stream has finished, and runs on a separate copy stream, so the next
+ * frame (into another canvas) renders while this one is copied out. The host
+ * buffers (pinned memory for an overlapped copy) must stay untouched until
+ * dg_canvas_read_wait returns. Any later operation on this canvas is ordered
+ * after the copy. */
+dg_status dg_canvas_read_async(dg_ctx* ctx, int32_t canvas, uint8_t* bgra, float* depth);
+/* Waits for the canvas's last dg_canvas_read_async; returns the error word of
+ * the frames it waited for (without clearing it). */
+dg_status dg_canvas_read_wait(dg_ctx* ctx, int32_t canvas);
 dg_status dg_canvas_write(dg_ctx* ctx, int32_t canvas, const uint8_t* bgra, const float* depth);
 /* Canvas::draw_triangle (canvas.rs:435-575), the GUI's 2D triangles, n of them
  * drawn in order: verts holds n x 3 vertices of 8 floats (x, y, u, v, r, g, b,

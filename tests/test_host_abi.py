@@ -138,6 +138,8 @@ def test_host_only_context_refuses_device_work(lib):
     assert lib.dg_scene_create(h, 0, 8, ctypes.byref(out)) == 1
     assert lib.dg_scene_set_lights(h, 0, None, 0) == 1
     assert lib.dg_status_string(3) == b"texel offset outside the texture map"
+    assert lib.dg_canvas_read_async(h, 0, None, None) == 1  # no such canvas
+    assert lib.dg_canvas_read_wait(h, 0) == 1
     n = ctypes.c_uint64()
     assert lib.dg_check_division(h, 1, 16, 1, ctypes.byref(n), None, None) == 6
     assert lib.dg_check_division(h, 4, 16, 1, ctypes.byref(n), None, None) == 1  # no such sample family
