@@ -57,3 +57,30 @@ def test_read_wait_without_async_read_returns(gpu_ctx):
     a.canvas.read_async(bgra, None)
     a.canvas.read_wait()
     assert np.array_equal(bgra, a.canvas.read(depth=False)[0])
+
+
+def test_graph_batch_replay_waits_for_pending_copy(gpu_ctx):
+    """A graph replay that renders into a canvas with a copy in flight is ordered
+    after the copy: the copy holds the frame rendered before the replay."""
+    from draw_gb300 import renderer
+
+    frames = S.batch_frames(n_frames=3, seed=17, side_range=(96, 160), tri_range=(2_000, 20_000), tex_range=(64, 64))
+    built = [renderer.build_scene(d, gpu_ctx) for d in frames]
+    batch = gpu_ctx.batch([b.scene for b in built], [b.canvas for b in built])
+    try:
+        batch.render()
+        refs = [b.canvas.read() for b in built]
+        pins = [_pinned(b.canvas.height, b.canvas.width) for b in built]
+        for b, p in zip(built, pins):
+            b.canvas.read_async(*p)
+        for d, b in zip(frames, built):  # move the cameras: the next replay draws different frames
+            b.scene.camera.reset(tuple(np.float32(c) * np.float32(1.2) for c in d.cam_pos), d.cam_dir,
+                                 float(d.ratio), d.near, d.far, d.fov_x)
+        batch.render()
+        for b, p, ref in zip(built, pins, refs):
+            b.canvas.read_wait()
+            assert np.array_equal(p[0], ref[0]) and np.array_equal(p[1].view(np.uint32), ref[1].view(np.uint32))
+        moved = [b.canvas.read()[0] for b in built]
+        assert any(not np.array_equal(m, r[0]) for m, r in zip(moved, refs))
+    finally:
+        batch.close()
