@@ -402,6 +402,8 @@ __device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uin
 
 __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
     __shared__ uint32_t s_bx[8][64], s_by[8][64];  // per-warp candidate buffers
+    __shared__ uint32_t s_sorted[256];             // a group of small triangles in box-size order
+    __shared__ uint32_t s_bucket[16];              // their counts, then offsets, per box-size class
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t* bx = s_bx[threadIdx.x >> 5];
@@ -423,10 +425,53 @@ __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
     const uint32_t nitems = (uint32_t)(ni64 < job.items_cap ? ni64 : job.items_cap);
     const unsigned long long ns64 = __ldcg(job.cnt + DG_CNT_SMALL);
     const uint32_t nsmall = (uint32_t)(ns64 < job.small_cap ? ns64 : job.small_cap);
-    const uint32_t nchunks = (nsmall + 31u) >> 5;
-    // Work index wi: chunks of 32 small triangles first (wi < nchunks), then the work items.
+    // Small triangles: one per lane, rasterized by that lane. When there are at
+    // least 32 per warp of the grid, a block takes 256 at a time and orders them by
+    // box-size class (the bit length of the box's pixel count) in shared memory, so
+    // that the lanes of a warp loop over boxes of about the same size
+    // (block-uniform loop); fewer go in chunks of 32 to single warps, ahead of the
+    // work items.
+    const bool sort_small = nsmall >= nwarps * 32u;
+    const uint32_t nsgroups = sort_small ? (nsmall + 255u) >> 8 : 0u;
+    for (uint32_t gi = blockIdx.x; gi < nsgroups; gi += gridDim.x) {
+        if (threadIdx.x < 16u) s_bucket[threadIdx.x] = 0u;
+        __syncthreads();
+        const uint32_t i = (gi << 8) + threadIdx.x;
+        uint32_t cls = 15u, rank = 0;
+        if (i < nsmall) {
+            const uint4 q1 = __ldcg(reinterpret_cast<const uint4*>(job.small + i) + 1);
+            const uint32_t px = q1.y * q1.z;  // at most small_max_px (<= 4096)
+            cls = 32u - __clz(px);            // 0..13
+            rank = atomicAdd(&s_bucket[cls], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {  // exclusive offsets of the classes; class 15 (no triangle) last
+            uint32_t run = 0;
+            for (uint32_t c = 0; c < 16u; c++) {
+                const uint32_t n = s_bucket[c];
+                s_bucket[c] = run;
+                run += n;
+            }
+        }
+        __syncthreads();
+        if (i < nsmall) s_sorted[s_bucket[cls] + rank] = i;
+        __syncthreads();
+        const uint32_t nin = nsmall - (gi << 8) < 256u ? nsmall - (gi << 8) : 256u;
+        if (threadIdx.x < nin) {
+            const uint4* qs = reinterpret_cast<const uint4*>(job.small + s_sorted[threadIdx.x]);
+            const uint4 q0 = __ldcg(qs), q1 = __ldcg(qs + 1);
+            const DgTriRec* R = job.trec + q0.x;
+            EdgeSet e;
+            load_edges(R, e);
+            const float4 dd = __ldg(reinterpret_cast<const float4*>(R) + 4);
+            raster_box(e, dd.x, dd.y, dd.z, q0.y, q0.w, q1.x, q1.y, q1.z, job.frames[q0.z]);
+        }
+        __syncthreads();  // s_bucket and s_sorted are reused by the next group
+    }
+    // Work index wi: chunks of 32 small triangles (wi < nchunks), then the work items.
+    const uint32_t nchunks = sort_small ? 0u : (nsmall + 31u) >> 5;
     for (uint32_t wi = warp; wi < nchunks + nitems; wi += nwarps) {
-        if (wi < nchunks) {  // one small triangle per lane, rasterized by that lane
+        if (wi < nchunks) {
             const uint32_t i = (wi << 5) + lane;
             if (i < nsmall) {
                 const uint4* qs = reinterpret_cast<const uint4*>(job.small + i);

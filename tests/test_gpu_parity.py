@@ -140,3 +140,27 @@ def test_parity_stress_config(gpu_ctx, oracle_lib):
             assert p.ok and p.n_covered > 500_000, f"{knobs}: {describe(p)}; {first_mismatch(ref, got)}"
     finally:
         gpu_ctx.set_tuning(**before)
+
+
+def test_small_triangle_sorting_keeps_results(gpu_ctx, oracle_lib):
+    """Small triangles go to per-lane rasterization in box-size order once there are
+    at least 32 per warp of the queue grid (a grid of one block per SM makes a
+    200k-triangle micro-sphere field take that path), in plain 32-triangle chunks
+    otherwise; both give the oracle's frame."""
+    desc = S.micro_sphere_field(width=640, height=360, n_tris=200_000, tex=256, n_lights=2)
+    ref = oracle_render(desc)
+    before = gpu_ctx.get_tuning()
+    try:
+        for knobs, sorted_path in ((dict(small_max_px=64, queue_blocks_per_sm=1), True),
+                                   (dict(small_max_px=64, queue_blocks_per_sm=64), False)):
+            gpu_ctx.set_tuning(**before)
+            gpu_ctx.set_tuning(**knobs)
+            got = gpu_render(desc, gpu_ctx)
+            p = compare(ref, got, desc.clear_depth)
+            assert p.ok, f"{knobs}: {describe(p)}; {first_mismatch(ref, got)}"
+            import torch
+
+            warps = torch.cuda.get_device_properties(0).multi_processor_count * knobs["queue_blocks_per_sm"] * 8
+            assert (gpu_ctx.last_stats()["small_triangles"] >= warps * 32) == sorted_path
+    finally:
+        gpu_ctx.set_tuning(**before)
