@@ -595,6 +595,48 @@ __device__ __forceinline__ void raster_box(const EdgeSet& e, float da, float db,
     uint32_t x = xlo, y = ylo;
     const uint32_t xe = xlo + w;
     const uint64_t n = (uint64_t)w * h;
+    if ((e.tie & DG_EDGE_FAST) && n <= 64u) {
+        // Two passes: the division-free sign test of every box pixel into a mask,
+        // then the covered pixels alone (divisions, depth, keyed minimum), so that
+        // a lane's expensive steps are not interleaved with its uncovered pixels.
+        uint64_t mask = 0;
+        for (uint32_t k = 0; k < (uint32_t)n; k++) {
+            const float xf = (float)x, yf = (float)y;
+            if (covered_signs(e.tie, edge_eval(e, 0, xf, yf), edge_eval(e, 1, xf, yf), edge_eval(e, 2, xf, yf)))
+                mask |= 1ull << k;
+            if (++x == xe) {
+                x = xlo;
+                y++;
+            }
+        }
+        if (!mask) return;
+        const bool rcp = edge_rcp_ok(e);
+        const float y0 = rcp ? __frcp_rn(e.den[0]) : 0.0f, y1 = rcp ? __frcp_rn(e.den[1]) : 0.0f,
+                    y2 = rcp ? __frcp_rn(e.den[2]) : 0.0f;
+        // k / w for k < 64 and w <= 64: k * ceil(2^16 / w) >> 16 errs by less than
+        // 64 / 2^16 < 1 / w, which cannot carry past the next multiple of 1 / w
+        const uint32_t inv_w = (65536u + w - 1u) / w;
+        while (mask) {
+            const uint32_t k = (uint32_t)__ffsll((long long)mask) - 1u;
+            mask &= mask - 1ull;
+            const uint32_t dy = (k * inv_w) >> 16, px = xlo + (k - dy * w), py = ylo + dy;
+            const float xf = (float)px, yf = (float)py;
+            const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
+            float al, be, ga;
+            if (rcp) {
+                al = div_rcp(n0, e.den[0], y0);
+                be = div_rcp(n1, e.den[1], y1);
+                ga = div_rcp(n2, e.den[2], y2);
+            } else {
+                al = fD(n0, e.den[0]);
+                be = fD(n1, e.den[1]);
+                ga = fD(n2, e.den[2]);
+            }
+            const float depth = interp(al, be, ga, da, db, dc);
+            if (depth < clear_depth) atomicMin(vis + (uint64_t)py * width + px, depth_key(depth, seq));
+        }
+        return;
+    }
     for (uint64_t k = 0; k < n; k++) {
         float al, be, ga;
         if (covered(e, (float)x, (float)y, al, be, ga)) {
