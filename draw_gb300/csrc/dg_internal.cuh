@@ -241,6 +241,7 @@ struct DgLaunchCfg {
     DgTransparentPlan tplan;
 };
 #define DG_SETUP_BLOCKS_PER_SM 4u
+#define DG_CLIP_DEFER 512u  // k_setup_raster: clipped survivors a block sets up in its second pass
 #define DG_QUEUE_BLOCKS_PER_SM 8u
 #define DG_CULL_BLOCKS_PER_SM 32u
 #define DG_NKERNELS 5  // vertex, cull, setup_raster, queue_raster, resolve (+ the transparent pass)

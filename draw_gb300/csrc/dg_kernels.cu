@@ -136,229 +136,257 @@ __device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* c, 
 
 __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
     __shared__ uint32_t s_records;  // statistics: record requests of the block
-    if (threadIdx.x == 0) s_records = 0u;
+    __shared__ uint32_t s_nclip;    // clipped survivors the block deferred
+    __shared__ uint32_t s_clip_i[DG_CLIP_DEFER], s_clip_g[DG_CLIP_DEFER];  // their survivor slots and indices
+    if (threadIdx.x == 0) {
+        s_records = 0u;
+        s_nclip = 0u;
+    }
     __syncthreads();
     wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long ns64 = __ldcg(job.cnt + DG_CNT_SURV);
     const uint32_t nsurv = (uint32_t)(ns64 < job.total_tri ? ns64 : job.total_tri);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nsurv; base += stride) {
-        const uint32_t i = base + lane;
-        int nout = 0;
-        uint32_t g = 0, si = 0, t = 0, row0 = 0, nrows = 0;
-        uint4 tp = make_uint4(0, 0, 0, 0), tuv = tp, tnr = tp;
-        float4 r[3];
-        bool clipped = false;
-        ClipProg P;  // built once per clipped triangle, used by every output
-        if (i < nsurv) {
-            g = __ldcg(job.surv + i);
-            si = seg_of_tri(job, g);
-            const DgSegDev& sg = job.segs[si];
-            t = g - sg.tri_begin;
-            tp = __ldg(sg.tri_pos + t);
-            tuv = __ldg(sg.tri_uv + t);  // for the triangle record, loaded alongside the vertex records
-            tnr = __ldg(sg.tri_nrm + t);
-            triangle_vertices(job, sg, job.frames[sg.frame], tp, r);
-            const uint32_t m = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
-            if ((m & 0x3u) == 0x3u) {
-                nout = 1;  // inside near and far: the triangle passes unchanged
-            } else {
-                const DgFrameDev& fr = job.frames[sg.frame];
-                float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
-                build_clip(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z}, P);
-                nout = P.nout;
-                clipped = true;
-                if (nout > 0 && P.nv > 3) nrows = (uint32_t)(P.nv - 3);  // light rows for the new vertices
-            }
-            if (nout > 0) {  // its vertices need light/halfway vectors for shading
-                const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
-                for (int k = 0; k < 3; k++) job.vmark[vv[k]] = 1u;  // plain stores: every writer writes 1
-            }
+    // Pass 0 sets up the survivors, strided over the grid, but defers those that
+    // need near/far clipping (up to DG_CLIP_DEFER per block) to pass 1, where the
+    // block's warps set them up 32 at a time: the long clip path then runs with
+    // all lanes busy instead of holding a warp of mostly unclipped lanes. Both
+    // passes are block-uniform (pass 1 starts after a barrier).
+    for (int pass = 0; pass < 2; pass++) {
+        uint32_t lim = nsurv, start = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u, step = gridDim.x * blockDim.x;
+        if (pass == 1) {
+            __syncthreads();
+            lim = s_nclip < DG_CLIP_DEFER ? s_nclip : DG_CLIP_DEFER;
+            start = threadIdx.x & ~31u;
+            step = blockDim.x;
         }
-        // Rows of the light/halfway table for clip vertices, one atomic per warp.
-        {
-            const unsigned long long r0 = warp_alloc(job.cnt + DG_CNT_VROW, nrows);
-            if (nrows != 0u) {
-                if (r0 + nrows <= job.vrow_extra) {
-                    row0 = (uint32_t)r0;
-                    clip_shade_rows(job, job.frames[job.segs[si].frame], P, job.total_vtx + row0);
-                } else {
-                    nrows = DG_NONE;  // no room: the fallback pass shades these pixels the long way
-                }
+        for (uint32_t base = start; base < lim; base += step) {
+            const bool valid = base + lane < lim;
+            uint32_t i = base + lane, g = 0;
+            if (pass == 1) {
+                i = valid ? s_clip_i[base + lane] : 0u;
+                g = valid ? s_clip_g[base + lane] : 0u;
+            } else if (valid) {
+                g = __ldcg(job.surv + i);
             }
-        }
-        // Triangle records: a triangle with one output uses record i (its survivor
-        // slot); the clip outputs of one with more take consecutive records after
-        // the first total_tri (one atomic per warp).
-        uint32_t rbase = DG_NONE;
-        {
-            const uint32_t multi = (nout > 1 && nrows != DG_NONE) ? (uint32_t)nout : 0u;
-            const unsigned long long rb = (unsigned long long)job.total_tri + warp_alloc(job.cnt + DG_CNT_TRECX, multi);
-            if (nout == 1 && nrows != DG_NONE) {
-                if (i < job.trec_cap) rbase = i;
-            } else if (multi && rb + (unsigned long long)nout <= job.trec_cap) {
-                rbase = (uint32_t)rb;
-            }
-        }
-        {
-            const uint32_t nrec = __reduce_add_sync(FULL, (uint32_t)nout);
-            if (lane == 0u && nrec) atomicAdd(&s_records, nrec);  // 32-bit shared atomic, one per warp
-        }
-        if (i < nsurv) job.rec_of[g] = rbase;
-
-        for (int rr = 0;; rr++) {
-            bool has = rr < nout;
-            if (__ballot_sync(FULL, has) == 0u) break;
-            RTri tr;
-            EdgeSet e;
-            bool small = false;  // goes to the small-triangle list
-            uint32_t nu = 0;     // work units to queue (0: not queued)
-            uint32_t qpx = 0;    // bounding-box pixels of the queued triangle
-            bool inplace = false;
-            tr.xlo = tr.xhi = tr.ylo = tr.yhi = 0;
-            tr.frame = 0;
-            if (has) {
+            int nout = 0;
+            uint32_t si = 0, t = 0, row0 = 0, nrows = 0;
+            uint4 tp = make_uint4(0, 0, 0, 0), tuv = tp, tnr = tp;
+            float4 r[3];
+            bool clipped = false;
+            ClipProg P;  // built once per clipped triangle, used by every output
+            if (valid) {
+                si = seg_of_tri(job, g);
                 const DgSegDev& sg = job.segs[si];
-                const DgFrameDev& fr = job.frames[sg.frame];
-                tr.frame = sg.frame;
-                tr.seq = ((sg.seq_base + t) << 2) | (uint32_t)rr;
-                if (!clipped) {
-                    tr.ax = r[0].x; tr.ay = r[0].y;
-                    tr.bx = r[1].x; tr.by = r[1].y;
-                    tr.cx = r[2].x; tr.cy = r[2].y;
-                    tr.da = r[0].z; tr.db = r[1].z; tr.dc = r[2].z;
+                t = g - sg.tri_begin;
+                tp = __ldg(sg.tri_pos + t);
+                tuv = __ldg(sg.tri_uv + t);  // for the triangle record, loaded alongside the vertex records
+                tnr = __ldg(sg.tri_nrm + t);
+                triangle_vertices(job, sg, job.frames[sg.frame], tp, r);
+                const uint32_t m = __float_as_uint(r[0].w) & __float_as_uint(r[1].w) & __float_as_uint(r[2].w);
+                uint32_t dslot = DG_CLIP_DEFER;
+                if ((m & 0x3u) == 0x3u) {
+                    nout = 1;  // inside near and far: the triangle passes unchanged
+                } else if (pass == 0 && (dslot = atomicAdd(&s_nclip, 1u)) < DG_CLIP_DEFER) {
+                    s_clip_i[dslot] = i;  // set up in pass 1 (nout stays 0 here)
+                    s_clip_g[dslot] = g;
                 } else {
-                    clip_output_tri(fr, P, rr, r, tr);
+                    const DgFrameDev& fr = job.frames[sg.frame];
+                    float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
+                    build_clip(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z}, P);
+                    nout = P.nout;
+                    clipped = true;
+                    if (nout > 0 && P.nv > 3) nrows = (uint32_t)(P.nv - 3);  // light rows for the new vertices
                 }
-                bool nan = isnan(tr.ax) || isnan(tr.ay) || isnan(tr.bx) || isnan(tr.by) || isnan(tr.cx) ||
-                           isnan(tr.cy);
-                if (!nan) {  // any NaN centre makes every barycentric NaN: nothing is covered
-                    bbox_axis(tr.ax, tr.bx, tr.cx, fr.width, tr.xlo, tr.xhi);
-                    bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
-                    make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
-                    if (rbase != DG_NONE) {
-                        if (!clipped)
-                            write_record(job, job.trec + rbase, sg, tp, tuv, tnr, e, r);
-                        else
-                            write_clip_record(job, job.trec + rbase + (uint32_t)rr, sg, tp, tuv, tnr, e, tr, P, rr,
-                                              job.total_vtx + row0);
-                    }
-                    uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
-                    if (rbase == DG_NONE) {
-                        inplace = true;
-                    } else if (px <= job.small_max_px) {
-                        small = true;
+                if (nout > 0) {  // its vertices need light/halfway vectors for shading
+                    const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
+                    for (int k = 0; k < 3; k++) job.vmark[vv[k]] = 1u;  // plain stores: every writer writes 1
+                }
+            }
+            // Rows of the light/halfway table for clip vertices, one atomic per warp.
+            {
+                const unsigned long long r0 = warp_alloc(job.cnt + DG_CNT_VROW, nrows);
+                if (nrows != 0u) {
+                    if (r0 + nrows <= job.vrow_extra) {
+                        row0 = (uint32_t)r0;
+                        clip_shade_rows(job, job.frames[job.segs[si].frame], P, job.total_vtx + row0);
                     } else {
-                        qpx = (uint32_t)px;  // below 2^31: the canvas has fewer pixels
-                        nu = (uint32_t)((px + DG_UNIT_PX - 1u) / DG_UNIT_PX);
+                        nrows = DG_NONE;  // no room: the fallback pass shades these pixels the long way
                     }
                 }
             }
-            // Queue this round's large triangles with one 64-bit atomic per warp: it hands out
-            // the queue records and their work items together; the warp then writes all its
-            // items, each lane taking every 32nd.
-            const unsigned qmask = __ballot_sync(FULL, nu != 0u);
-            if (qmask) {
-                const uint32_t ni = (nu + job.item_units - 1u) / job.item_units;
-                uint32_t incl = ni, uincl = nu;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t v = __shfl_up_sync(FULL, incl, o);
-                    const uint32_t vu = __shfl_up_sync(FULL, uincl, o);
-                    if (lane >= (uint32_t)o) {
-                        incl += v;
-                        uincl += vu;
-                    }
-                }
-                const uint32_t total_items = __shfl_sync(FULL, incl, 31);
-                const uint32_t total_units = __shfl_sync(FULL, uincl, 31);
-                const int leader = __ffs(qmask) - 1;
-                unsigned long long old = 0;
-                if ((int)lane == leader) {
-                    old = atomicAdd(job.cnt + DG_CNT_QUEUE,
-                                    ((unsigned long long)__popc(qmask) << DG_PACK_SHIFT) | total_items);
-                    atomicAdd(job.cnt + DG_CNT_UNITS, (unsigned long long)total_units);
-                }
-                old = __shfl_sync(FULL, old, leader);
-                const uint64_t rec = (old >> DG_PACK_SHIFT) + __popc(qmask & ((1u << lane) - 1u));
-                const uint64_t ibase = (old & ((1ull << DG_PACK_SHIFT) - 1ull)) + (incl - ni);
-                const bool fits = nu != 0u && rec < job.queue_cap && ibase + ni <= job.items_cap;
-                if (fits) {
-                    uint4* qd = reinterpret_cast<uint4*>(job.queue + rec);
-                    qd[0] = make_uint4(rbase + (uint32_t)rr, tr.seq, tr.frame, tr.xlo);
-                    qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, qpx, nu);
-                } else if (nu != 0u) {
-                    inplace = true;  // queue full: this lane rasterizes the box itself
-                }
-                // Items of a lane that did not fit are marked empty (their slots are handed out).
-                // Lanes with at least 32 items: the whole warp writes them, one lane after another.
-                unsigned big = __ballot_sync(FULL, ni >= 32u);
-                while (big) {
-                    const int L = __ffs(big) - 1;
-                    big &= big - 1u;
-                    const uint32_t lni = __shfl_sync(FULL, ni, L);
-                    const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, L);
-                    const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, L);
-                    const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, L) != 0u;
-                    for (uint32_t k = lane; k < lni; k += 32u)
-                        if (oib + k < job.items_cap)
-                            job.items[oib + k] = ofits ? make_uint2(orec, k * job.item_units) : make_uint2(DG_NONE, 0u);
-                }
-                // The other lanes' items numbered together: item j belongs to the first lane
-                // whose inclusive count exceeds it.
-                const uint32_t ns = ni < 32u ? ni : 0u;
-                uint32_t sincl = ns;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t v = __shfl_up_sync(FULL, sincl, o);
-                    if (lane >= (uint32_t)o) sincl += v;
-                }
-                const uint32_t stotal = __shfl_sync(FULL, sincl, 31);
-                const uint32_t sexcl = sincl - ns;
-                for (uint32_t b0 = 0; b0 < stotal; b0 += 32u) {
-                    const uint32_t j = b0 + lane;
-                    int lo = 0, hi = 31;
-#pragma unroll
-                    for (int it = 0; it < 5; it++) {
-                        const int mid = (lo + hi) >> 1;
-                        if (__shfl_sync(FULL, sincl, mid) > j)
-                            hi = mid;
-                        else
-                            lo = mid + 1;
-                    }
-                    const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, lo);
-                    const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, lo);
-                    const uint32_t oex = __shfl_sync(FULL, sexcl, lo);
-                    const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, lo) != 0u;
-                    const uint32_t k = j - oex;  // item index within its record
-                    if (j < stotal && oib + k < job.items_cap)
-                        job.items[oib + k] = ofits ? make_uint2(orec, k * job.item_units) : make_uint2(DG_NONE, 0u);
+            // Triangle records: a triangle with one output uses record i (its survivor
+            // slot); the clip outputs of one with more take consecutive records after
+            // the first total_tri (one atomic per warp).
+            uint32_t rbase = DG_NONE;
+            {
+                const uint32_t multi = (nout > 1 && nrows != DG_NONE) ? (uint32_t)nout : 0u;
+                const unsigned long long rb = (unsigned long long)job.total_tri + warp_alloc(job.cnt + DG_CNT_TRECX, multi);
+                if (nout == 1 && nrows != DG_NONE) {
+                    if (i < job.trec_cap) rbase = i;
+                } else if (multi && rb + (unsigned long long)nout <= job.trec_cap) {
+                    rbase = (uint32_t)rb;
                 }
             }
-            // Small triangles go to the small-triangle list (one atomic per warp), which the
-            // queue pass rasterizes one triangle per lane.
-            const unsigned smask = __ballot_sync(FULL, small);
-            if (smask) {
-                const int leader = __ffs(smask) - 1;
-                unsigned long long old = 0;
-                if ((int)lane == leader) old = atomicAdd(job.cnt + DG_CNT_SMALL, (unsigned long long)__popc(smask));
-                old = __shfl_sync(FULL, old, leader);
-                const uint64_t slot = old + __popc(smask & ((1u << lane) - 1u));
-                if (small) {
-                    if (slot < job.small_cap) {
-                        uint4* qd = reinterpret_cast<uint4*>(job.small + slot);
+            {
+                const uint32_t nrec = __reduce_add_sync(FULL, (uint32_t)nout);
+                if (lane == 0u && nrec) atomicAdd(&s_records, nrec);  // 32-bit shared atomic, one per warp
+            }
+            if (valid) job.rec_of[g] = rbase;  // a deferred triangle's entry is rewritten in pass 1
+
+            for (int rr = 0;; rr++) {
+                bool has = rr < nout;
+                if (__ballot_sync(FULL, has) == 0u) break;
+                RTri tr;
+                EdgeSet e;
+                bool small = false;  // goes to the small-triangle list
+                uint32_t nu = 0;     // work units to queue (0: not queued)
+                uint32_t qpx = 0;    // bounding-box pixels of the queued triangle
+                bool inplace = false;
+                tr.xlo = tr.xhi = tr.ylo = tr.yhi = 0;
+                tr.frame = 0;
+                if (has) {
+                    const DgSegDev& sg = job.segs[si];
+                    const DgFrameDev& fr = job.frames[sg.frame];
+                    tr.frame = sg.frame;
+                    tr.seq = ((sg.seq_base + t) << 2) | (uint32_t)rr;
+                    if (!clipped) {
+                        tr.ax = r[0].x; tr.ay = r[0].y;
+                        tr.bx = r[1].x; tr.by = r[1].y;
+                        tr.cx = r[2].x; tr.cy = r[2].y;
+                        tr.da = r[0].z; tr.db = r[1].z; tr.dc = r[2].z;
+                    } else {
+                        clip_output_tri(fr, P, rr, r, tr);
+                    }
+                    bool nan = isnan(tr.ax) || isnan(tr.ay) || isnan(tr.bx) || isnan(tr.by) || isnan(tr.cx) ||
+                               isnan(tr.cy);
+                    if (!nan) {  // any NaN centre makes every barycentric NaN: nothing is covered
+                        bbox_axis(tr.ax, tr.bx, tr.cx, fr.width, tr.xlo, tr.xhi);
+                        bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
+                        make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
+                        if (rbase != DG_NONE) {
+                            if (!clipped)
+                                write_record(job, job.trec + rbase, sg, tp, tuv, tnr, e, r);
+                            else
+                                write_clip_record(job, job.trec + rbase + (uint32_t)rr, sg, tp, tuv, tnr, e, tr, P, rr,
+                                                  job.total_vtx + row0);
+                        }
+                        uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
+                        if (rbase == DG_NONE) {
+                            inplace = true;
+                        } else if (px <= job.small_max_px) {
+                            small = true;
+                        } else {
+                            qpx = (uint32_t)px;  // below 2^31: the canvas has fewer pixels
+                            nu = (uint32_t)((px + DG_UNIT_PX - 1u) / DG_UNIT_PX);
+                        }
+                    }
+                }
+                // Queue this round's large triangles with one 64-bit atomic per warp: it hands out
+                // the queue records and their work items together; the warp then writes all its
+                // items, each lane taking every 32nd.
+                const unsigned qmask = __ballot_sync(FULL, nu != 0u);
+                if (qmask) {
+                    const uint32_t ni = (nu + job.item_units - 1u) / job.item_units;
+                    uint32_t incl = ni, uincl = nu;
+    #pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+                        const uint32_t vu = __shfl_up_sync(FULL, uincl, o);
+                        if (lane >= (uint32_t)o) {
+                            incl += v;
+                            uincl += vu;
+                        }
+                    }
+                    const uint32_t total_items = __shfl_sync(FULL, incl, 31);
+                    const uint32_t total_units = __shfl_sync(FULL, uincl, 31);
+                    const int leader = __ffs(qmask) - 1;
+                    unsigned long long old = 0;
+                    if ((int)lane == leader) {
+                        old = atomicAdd(job.cnt + DG_CNT_QUEUE,
+                                        ((unsigned long long)__popc(qmask) << DG_PACK_SHIFT) | total_items);
+                        atomicAdd(job.cnt + DG_CNT_UNITS, (unsigned long long)total_units);
+                    }
+                    old = __shfl_sync(FULL, old, leader);
+                    const uint64_t rec = (old >> DG_PACK_SHIFT) + __popc(qmask & ((1u << lane) - 1u));
+                    const uint64_t ibase = (old & ((1ull << DG_PACK_SHIFT) - 1ull)) + (incl - ni);
+                    const bool fits = nu != 0u && rec < job.queue_cap && ibase + ni <= job.items_cap;
+                    if (fits) {
+                        uint4* qd = reinterpret_cast<uint4*>(job.queue + rec);
                         qd[0] = make_uint4(rbase + (uint32_t)rr, tr.seq, tr.frame, tr.xlo);
-                        qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, tr.yhi - tr.ylo + 1u, 0u);
-                    } else {
-                        inplace = true;  // list full
+                        qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, qpx, nu);
+                    } else if (nu != 0u) {
+                        inplace = true;  // queue full: this lane rasterizes the box itself
+                    }
+                    // Items of a lane that did not fit are marked empty (their slots are handed out).
+                    // Lanes with at least 32 items: the whole warp writes them, one lane after another.
+                    unsigned big = __ballot_sync(FULL, ni >= 32u);
+                    while (big) {
+                        const int L = __ffs(big) - 1;
+                        big &= big - 1u;
+                        const uint32_t lni = __shfl_sync(FULL, ni, L);
+                        const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, L);
+                        const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, L);
+                        const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, L) != 0u;
+                        for (uint32_t k = lane; k < lni; k += 32u)
+                            if (oib + k < job.items_cap)
+                                job.items[oib + k] = ofits ? make_uint2(orec, k * job.item_units) : make_uint2(DG_NONE, 0u);
+                    }
+                    // The other lanes' items numbered together: item j belongs to the first lane
+                    // whose inclusive count exceeds it.
+                    const uint32_t ns = ni < 32u ? ni : 0u;
+                    uint32_t sincl = ns;
+    #pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t v = __shfl_up_sync(FULL, sincl, o);
+                        if (lane >= (uint32_t)o) sincl += v;
+                    }
+                    const uint32_t stotal = __shfl_sync(FULL, sincl, 31);
+                    const uint32_t sexcl = sincl - ns;
+                    for (uint32_t b0 = 0; b0 < stotal; b0 += 32u) {
+                        const uint32_t j = b0 + lane;
+                        int lo = 0, hi = 31;
+    #pragma unroll
+                        for (int it = 0; it < 5; it++) {
+                            const int mid = (lo + hi) >> 1;
+                            if (__shfl_sync(FULL, sincl, mid) > j)
+                                hi = mid;
+                            else
+                                lo = mid + 1;
+                        }
+                        const uint32_t orec = (uint32_t)__shfl_sync(FULL, (unsigned long long)rec, lo);
+                        const uint64_t oib = __shfl_sync(FULL, (unsigned long long)ibase, lo);
+                        const uint32_t oex = __shfl_sync(FULL, sexcl, lo);
+                        const bool ofits = __shfl_sync(FULL, fits ? 1u : 0u, lo) != 0u;
+                        const uint32_t k = j - oex;  // item index within its record
+                        if (j < stotal && oib + k < job.items_cap)
+                            job.items[oib + k] = ofits ? make_uint2(orec, k * job.item_units) : make_uint2(DG_NONE, 0u);
                     }
                 }
-            }
-            if (inplace) {  // this lane rasterizes the box itself
-                atomicAdd(job.cnt + DG_CNT_INPLACE, 1ull);
-                raster_box(e, tr.da, tr.db, tr.dc, tr.seq, tr.xlo, tr.ylo, tr.xhi - tr.xlo + 1u, tr.yhi - tr.ylo + 1u,
-                           job.frames[tr.frame]);
+                // Small triangles go to the small-triangle list (one atomic per warp), which the
+                // queue pass rasterizes one triangle per lane.
+                const unsigned smask = __ballot_sync(FULL, small);
+                if (smask) {
+                    const int leader = __ffs(smask) - 1;
+                    unsigned long long old = 0;
+                    if ((int)lane == leader) old = atomicAdd(job.cnt + DG_CNT_SMALL, (unsigned long long)__popc(smask));
+                    old = __shfl_sync(FULL, old, leader);
+                    const uint64_t slot = old + __popc(smask & ((1u << lane) - 1u));
+                    if (small) {
+                        if (slot < job.small_cap) {
+                            uint4* qd = reinterpret_cast<uint4*>(job.small + slot);
+                            qd[0] = make_uint4(rbase + (uint32_t)rr, tr.seq, tr.frame, tr.xlo);
+                            qd[1] = make_uint4(tr.ylo, tr.xhi - tr.xlo + 1u, tr.yhi - tr.ylo + 1u, 0u);
+                        } else {
+                            inplace = true;  // list full
+                        }
+                    }
+                }
+                if (inplace) {  // this lane rasterizes the box itself
+                    atomicAdd(job.cnt + DG_CNT_INPLACE, 1ull);
+                    raster_box(e, tr.da, tr.db, tr.dc, tr.seq, tr.xlo, tr.ylo, tr.xhi - tr.xlo + 1u, tr.yhi - tr.ylo + 1u,
+                               job.frames[tr.frame]);
+                }
             }
         }
     }
