@@ -383,7 +383,6 @@ void slot_free(JobSlot& s) {
     dfree(s.d_vmark);
     dfree(s.d_queue);
     dfree(s.d_small);
-    dfree(s.d_fb);
     for (int k = 0; k < 2; k++) {
         dfree(s.d_tkey[k]); dfree(s.d_tval[k]); dfree(s.d_fkey[k]); dfree(s.d_fval[k]);
     }
@@ -470,13 +469,12 @@ uint64_t slot_scratch_after(const JobSlot& s, uint64_t V, uint64_t T, uint32_t L
     const size_t vmark = cap_after(s.vmark_cap, s.d_vmark, std::max<uint64_t>(V, 1));
     const size_t q = cap_after(s.queue_cap, s.d_queue, queue_records(T));
     const size_t sm = cap_after(s.small_cap, s.d_small, queue_records(T));
-    const size_t fb = cap_after(s.fb_cap, s.d_fb, P / ((uint64_t)DG_TILE_W * 8u) + 65536u);  // tiles, any tile_rows
     const size_t qb = cap_after(s.items_cap, s.d_items, dg_items_cap(q));
     const size_t sv = cap_after(s.surv_cap, s.d_surv, std::max<uint64_t>(T, 1));
     const size_t ro = cap_after(s.rec_of_cap, s.d_rec_of, std::max<uint64_t>(T, 1));
     const size_t tr = cap_after(s.trec_cap, s.d_trec, trec_records(T));
     return vmask * sizeof(uint16_t) + vrec * sizeof(float4) + vshade * sizeof(float4) + vmark * sizeof(uint8_t) + (q + sm) * sizeof(DgQueueRec) +
-           qb * sizeof(uint2) + (sv + ro + fb) * sizeof(uint32_t) + tr * sizeof(DgTriRec);
+           qb * sizeof(uint2) + (sv + ro) * sizeof(uint32_t) + tr * sizeof(DgTriRec);
 }
 
 dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarget* targets, uint32_t n,
@@ -651,8 +649,6 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         e = grow(S, &S.d_items, &S.items_cap, dg_items_cap(S.queue_cap));
         if (e) return e;
     }
-    e = grow(S, &S.d_fb, &S.fb_cap, std::max<uint64_t>(total_tiles, 1));
-    if (e) return e;
     if (S.small_cap < want_queue) {
         e = grow(S, &S.d_small, &S.small_cap, want_queue);
         if (e) return e;
@@ -689,11 +685,10 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.cnt = S.d_counters;
     job.total_px = (uint32_t)total_px;
     job.tile_rows = S.tile_rows;
-    job.fb_tiles = S.d_fb;
     job.tex = c->d_tex;
     job.ntex = (uint32_t)c->tex.size();
     job.err = S.d_err;
-    B.launches = (total_vtx ? 1 : 0) + (total_tri ? 3 : 0) + (total_tiles ? 2 : 0);
+    B.launches = (total_vtx ? 1 : 0) + (total_tri ? 3 : 0) + (total_tiles ? 1 : 0);
     B.cfg.tplan = DgTransparentPlan{};
     if (ntt) {
         job.ntt = (uint32_t)ntt;
@@ -738,7 +733,6 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     B.cfg.cull_blocks = (unsigned)c->nsm * S.cull_blocks_per_sm;
     B.cfg.setup_blocks = (unsigned)c->nsm * S.setup_blocks_per_sm;
     B.cfg.queue_blocks = (unsigned)c->nsm * S.queue_blocks_per_sm;
-    B.cfg.fallback_blocks = (unsigned)c->nsm;
     B.total_vtx = total_vtx;
     B.total_tri = total_tri;
     return DG_OK;

@@ -127,8 +127,6 @@ struct JobSlot {
     DgQueueRec* d_queue = nullptr;
     DgQueueRec* d_small = nullptr;  // small-triangle list
     size_t small_cap = 0;
-    uint32_t* d_fb = nullptr;  // resolve fallback tile list
-    size_t fb_cap = 0;
     // transparent pass scratch (DgJobDev)
     uint64_t* d_tkey[2] = {};
     uint32_t* d_tval[2] = {};

@@ -172,7 +172,6 @@ struct alignas(16) DgQueueRec {
 #define DG_CNT_UNITS 6    // work units of the queued triangles
 #define DG_CNT_SMALL 7    // entries of the small-triangle list
 #define DG_CNT_TRECX 8    // records handed out after the first total_tri (multi-output clips)
-#define DG_CNT_FBTILES 9  // entries of the fallback tile list
 #define DG_CNT_TFRAG 10   // transparent fragments emitted
 #define DG_NCOUNTERS 12
 
@@ -201,7 +200,6 @@ struct DgJobDev {
     uint32_t item_units;    // work units per raster work item (>= 1)
     uint32_t total_px;      // pixels of all frames
     uint32_t tile_rows;     // resolve tile height (8, 16 or 32)
-    uint32_t* fb_tiles;     // [total_tiles] tiles with pixels whose triangle has no record
     unsigned long long* cnt;  // DG_NCOUNTERS job counters, zero at the start of the job
     const DgTexDev* tex;
     uint32_t ntex;          // entries of tex
@@ -237,7 +235,6 @@ struct DgLaunchCfg {
     unsigned cull_blocks;   // grid caps / sizes in 256-thread blocks
     unsigned setup_blocks;
     unsigned queue_blocks;
-    unsigned fallback_blocks;
     DgTransparentPlan tplan;
 };
 #define DG_SETUP_BLOCKS_PER_SM 4u

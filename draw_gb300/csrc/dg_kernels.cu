@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                         row0 = (uint32_t)r0;
                         clip_shade_rows(job, job.frames[job.segs[si].frame], P, job.total_vtx + row0);
                     } else {
-                        nrows = DG_NONE;  // no room: the fallback pass shades these pixels the long way
+                        nrows = DG_NONE;  // no room: k_resolve shades these pixels the long way
                     }
                 }
             }
@@ -584,6 +584,44 @@ __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
     }
 }
 
+// Pixels of tile `tile` whose winning triangle has no record (the record
+// buffers were full) kept their keys in phase 1: they are shaded here from the
+// mesh (shade_without_record) and their keys reset. The tile's own CTA calls it
+// at the end of k_resolve, each thread on the pixels it read in phase 1. Out of
+// line, so that the long path costs the main path no registers (the job is a
+// __grid_constant__ parameter: its address needs no copy).
+template <uint32_t TH>
+__device__ __noinline__ void shade_tile_without_records(const DgJobDev& job, uint32_t tile, const float* inv255,
+                                                        const DgTexDev* stex) {
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
+    const DgFrameDev& fr = job.frames[fi];
+    const uint32_t lt = tile - fr.tile_begin;
+    const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
+    const uint32_t x = tx * DG_TILE_W + lane;
+    const uint32_t W = fr.width, H = fr.height;
+    uint32_t shaded = 0;
+    for (uint32_t j = 0; j < TH / 8u; j++) {
+        const uint32_t y = ty * TH + wid + 8u * j;
+        if (x >= W || y >= H) continue;
+        const uint64_t i = (uint64_t)y * W + x;
+        const uint64_t key = __ldcg(reinterpret_cast<const unsigned long long*>(fr.vis) + i);
+        if (key == DG_VIS_EMPTY) continue;  // empty, or shaded from its record
+        fr.vis[i] = DG_VIS_EMPTY;
+        float d = 0.0f;
+        int errc;
+        uint32_t c = shade_without_record(job, fr, (uint32_t)key, x, y, inv255, stex, d, errc);
+        if (errc != DG_OK) {
+            c = AZUL_BB;
+            atomicOr(job.err, 1u << errc);
+        }
+        fr.depth[i] = d;
+        fr.colour[(uint64_t)(H - 1u - y) * W + x] = c;
+        shaded++;
+    }
+    if (shaded) atomicAdd(job.cnt + DG_CNT_COVERED, (unsigned long long)shaded);
+}
+
 // Resolve and shade, fused: one 32 x TH tile per CTA of 256 threads (TH = 8,
 // 16 or 32: the tile_rows knob).
 //  1. Each thread reads the visibility keys of TH/8 pixels (rows r, r+8, ...
@@ -591,13 +629,13 @@ __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
 //     (this is Canvas::clear, canvas.rs:425-433); a covered one has its key
 //     reset for the next frame and goes into the tile's shade list in shared
 //     memory with its triangle record, in row-major order. A covered pixel
-//     whose triangle has no record keeps its key and the tile is listed for
-//     k_resolve_fallback.
+//     whose triangle has no record keeps its key for step 3.
 //  2. The CTA shades its list densely: the winning fragment of every covered
 //     pixel is shaded once (canvas.rs:682-741) and its colour (row H-1-y) and
 //     depth (y*W+x) are written (canvas.rs:923-930).
+//  3. If a pixel of the tile had no record, shade_tile_without_records.
 template <uint32_t TH>
-__global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
+__global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
     __shared__ float inv255[256];
     __shared__ DgTexDev stex[DG_SMEM_TEX];
     __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
@@ -652,7 +690,7 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
                 val[j] += o;
                 fr.vis[i] = DG_VIS_EMPTY;
             } else {
-                val[j] = DG_NONE;  // shaded by the fallback pass, which resets the key
+                val[j] = DG_NONE;  // shaded at the end, from the mesh, which resets the key
                 no_record = 1;
             }
         }
@@ -700,61 +738,8 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const DgJobDev job) {
         fr.depth[(uint64_t)py * W + px] = d;
         fr.colour[(uint64_t)(H - 1u - py) * W + px] = c;
     }
-    // a tile with pixels whose triangle has no record goes to the fallback pass
-    if (threadIdx.x == 0 && any_no_record) {
-        const unsigned long long slot = atomicAdd(job.cnt + DG_CNT_FBTILES, 1ull);
-        if (slot < job.total_tiles) job.fb_tiles[slot] = tile;
-    }
-}
-
-// Fallback pass of the resolve: pixels whose winning triangle has no record (the
-// record buffers were full) kept their keys in k_resolve; here the tiles that
-// hold such pixels are read again and those pixels are shaded from the mesh
-// (shade_without_record) and their keys reset. Exits at once when no tile
-// needs it.
-template <uint32_t TH>
-__global__ void __launch_bounds__(256) k_resolve_fallback(const DgJobDev job) {
-    __shared__ float inv255[256];
-    __shared__ DgTexDev stex[DG_SMEM_TEX];
-    wait_previous_kernel();
-    const unsigned long long n64 = __ldcg(job.cnt + DG_CNT_FBTILES);
-    const uint32_t ntiles = (uint32_t)(n64 < job.total_tiles ? n64 : job.total_tiles);
-    if (ntiles == 0u) return;
-    inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
-    const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
-    for (uint32_t i = threadIdx.x; i < nst * 3u; i += blockDim.x)
-        reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
-    __syncthreads();
-    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    uint32_t shaded = 0;
-    for (uint32_t ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-        const uint32_t tile = __ldcg(job.fb_tiles + ti);
-        const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
-        const DgFrameDev& fr = job.frames[fi];
-        const uint32_t lt = tile - fr.tile_begin;
-        const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
-        const uint32_t x = tx * DG_TILE_W + lane;
-        const uint32_t W = fr.width, H = fr.height;
-        for (uint32_t j = 0; j < TH / 8u; j++) {
-            const uint32_t y = ty * TH + wid + 8u * j;
-            if (x >= W || y >= H) continue;
-            const uint64_t i = (uint64_t)y * W + x;
-            const uint64_t key = __ldcg(reinterpret_cast<const unsigned long long*>(fr.vis) + i);
-            if (key == DG_VIS_EMPTY) continue;  // empty, or shaded by k_resolve
-            fr.vis[i] = DG_VIS_EMPTY;
-            float d = 0.0f;
-            int errc;
-            uint32_t c = shade_without_record(job, fr, (uint32_t)key, x, y, inv255, stex, d, errc);
-            if (errc != DG_OK) {
-                c = AZUL_BB;
-                atomicOr(job.err, 1u << errc);
-            }
-            fr.depth[i] = d;
-            fr.colour[(uint64_t)(H - 1u - y) * W + x] = c;
-            shaded++;
-        }
-    }
-    if (shaded) atomicAdd(job.cnt + DG_CNT_COVERED, (unsigned long long)shaded);
+    // pixels whose triangle has no record: shaded the long way (block-uniform)
+    if (any_no_record) shade_tile_without_records<TH>(job, tile, inv255, stex);
 }
 
 __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, float dv, int fc, int fd) {
@@ -812,10 +797,6 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
     if (job.total_tiles) {
         auto kr = job.tile_rows == 8u ? k_resolve<8> : job.tile_rows == 16u ? k_resolve<16> : k_resolve<32>;
         if ((e = launch_dependent(kr, job.total_tiles, 256, job, s)) != cudaSuccess) return e;
-        auto kf = job.tile_rows == 8u    ? k_resolve_fallback<8>
-                  : job.tile_rows == 16u ? k_resolve_fallback<16>
-                                         : k_resolve_fallback<32>;
-        if ((e = launch_dependent(kf, cfg.fallback_blocks, 256, job, s)) != cudaSuccess) return e;
     }
     // part 2: the ordered blend over the opaque colours
     if ((e = dg_launch_transparent(2, job, cfg.tplan, s)) != cudaSuccess) return e;

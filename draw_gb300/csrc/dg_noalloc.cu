@@ -43,9 +43,7 @@ constexpr size_t kOffQbase = align_up(kOffSmall + (size_t)kQueueCap * sizeof(DgQ
 constexpr size_t kOffSurv = align_up(kOffQbase + (size_t)dg_items_cap(kQueueCap) * sizeof(uint2));
 constexpr size_t kOffRecOf = align_up(kOffSurv + (size_t)DG_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t));
 constexpr size_t kOffTrec = align_up(kOffRecOf + (size_t)DG_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t));
-constexpr uint32_t kFbCap = 16384;  // resolve fallback tiles: more than a canvas within the pixel limit has
-constexpr size_t kOffFb = align_up(kOffTrec + (size_t)kTrecCap * sizeof(DgTriRec));
-constexpr size_t kOffCounters = align_up(kOffFb + (size_t)kFbCap * sizeof(uint32_t));
+constexpr size_t kOffCounters = align_up(kOffTrec + (size_t)kTrecCap * sizeof(DgTriRec));
 constexpr size_t kOffErr = align_up(kOffCounters + DG_NCOUNTERS * sizeof(unsigned long long));
 constexpr size_t kOffWhite = align_up(kOffErr + sizeof(uint32_t));
 constexpr size_t kOffVis = align_up(kOffWhite + 8);
@@ -146,7 +144,6 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     f.tiles_x = (p->canvas_width + DG_TILE_W - 1) / DG_TILE_W;
     f.pix_begin = 0;
     const uint32_t tiles = f.tiles_x * ((p->canvas_height + DG_TILE_H - 1) / DG_TILE_H);
-    if (tiles > kFbCap) return DG_E_LIMIT;  // not reachable within DG_NOALLOC_MAX_PIXELS
 
     DgSegDev& sg = d.seg;
     sg.frame = 0;
@@ -200,7 +197,6 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.total_vtx = m->nv;
     job.total_tri = m->ntri;
     job.total_tiles = tiles;
-    job.fb_tiles = reinterpret_cast<uint32_t*>(base + kOffFb);
     job.shade_stride = p->nlights;
     job.vrec = reinterpret_cast<float4*>(base + kOffVrec);
     job.vmask = reinterpret_cast<uint16_t*>(base + kOffVmask);
@@ -243,7 +239,6 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     cfg.cull_blocks = (unsigned)nsm * DG_CULL_BLOCKS_PER_SM;
     cfg.setup_blocks = (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM;
     cfg.queue_blocks = (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM;
-    cfg.fallback_blocks = (unsigned)nsm;
     NA_CUDA(dg_launch_job(job, cfg, s, nullptr));
 
     if (status_out) {

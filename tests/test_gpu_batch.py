@@ -35,7 +35,7 @@ def test_graph_batch_equals_oracle_across_replays(gpu_ctx, oracle_lib):
         _check(frames, built)
         info = batch.info()
         assert info["captures"] == 1 and info["replays"] == 2 and info["frames"] == len(frames)
-        assert info["kernels_per_replay"] == 6
+        assert info["kernels_per_replay"] == 5
         # moved cameras: the replay uploads new descriptors, no new capture
         for d, b in zip(frames, built):
             d.cam_pos = tuple(np.float32(c) * np.float32(1.25) for c in d.cam_pos)
