@@ -164,3 +164,23 @@ def test_small_triangle_sorting_keeps_results(gpu_ctx, oracle_lib):
             assert (gpu_ctx.last_stats()["small_triangles"] >= warps * 32) == sorted_path
     finally:
         gpu_ctx.set_tuning(**before)
+
+
+def test_clip_deferral_overflow_keeps_results(gpu_ctx, oracle_lib):
+    """Survivors that need near-plane clipping are set up in a second pass of each
+    setup block, up to 512 per block; beyond that a block clips them in the first
+    pass. Micro-spheres that all straddle the near plane, with one setup block per
+    SM, exercise both: the frame equals the oracle's."""
+    desc = S.micro_sphere_field(width=640, height=360, n_tris=1_000_000, tex=256, n_lights=2, slab=1.0)
+    ref = oracle_render(desc)
+    before = gpu_ctx.get_tuning()
+    try:
+        for knobs in (dict(setup_blocks_per_sm=1), dict(setup_blocks_per_sm=16)):
+            gpu_ctx.set_tuning(**before)
+            gpu_ctx.set_tuning(**knobs)
+            got = gpu_render(desc, gpu_ctx)
+            p = compare(ref, got, desc.clear_depth)
+            assert p.ok, f"{knobs}: {describe(p)}; {first_mismatch(ref, got)}"
+            assert gpu_ctx.last_stats()["clip_rows"] > 0
+    finally:
+        gpu_ctx.set_tuning(**before)
