@@ -297,6 +297,8 @@ void free_canvas(Canvas& v) {
     dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
     if (v.ev_rendered) cudaEventDestroy(v.ev_rendered);
     if (v.ev_read) cudaEventDestroy(v.ev_read);
+    if (v.h_err) cudaFreeHost(v.h_err);
+    v.h_err = nullptr;
     v.ev_rendered = v.ev_read = nullptr;
     v.read_pending = false;
 }
@@ -1305,11 +1307,15 @@ dg_status dg_canvas_read_async(dg_ctx* c, int32_t id, uint8_t* bgra, float* dept
     if (!c->copy_stream) DG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     if (!v->ev_rendered) DG_CUDA(cudaEventCreateWithFlags(&v->ev_rendered, cudaEventDisableTiming));
     if (!v->ev_read) DG_CUDA(cudaEventCreateWithFlags(&v->ev_read, cudaEventDisableTiming));
+    if (!v->h_err && cudaMallocHost((void**)&v->h_err, sizeof(uint32_t)) != cudaSuccess) return DG_E_OOM;
     const uint64_t n = v->w * v->h;
     DG_CUDA(cudaEventRecord(v->ev_rendered, c->main.stream));
     DG_CUDA(cudaStreamWaitEvent(c->copy_stream, v->ev_rendered, 0));
     if (bgra) DG_CUDA(cudaMemcpyAsync(bgra, v->d_colour, n * 4, cudaMemcpyDeviceToHost, c->copy_stream));
     if (depth) DG_CUDA(cudaMemcpyAsync(depth, v->d_depth, n * 4, cudaMemcpyDeviceToHost, c->copy_stream));
+    // the error word of the frames before the copy, read with it (not cleared:
+    // later frames may be running, and the next synchronous call reports it again)
+    DG_CUDA(cudaMemcpyAsync(v->h_err, c->main.d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->copy_stream));
     DG_CUDA(cudaEventRecord(v->ev_read, c->copy_stream));
     v->read_pending = true;
     return DG_OK;
@@ -1321,13 +1327,8 @@ dg_status dg_canvas_read_wait(dg_ctx* c, int32_t id) {
     dg_status e = set_device(c);
     if (e) return e;
     if (!v->ev_read) return DG_OK;  // never read asynchronously
-    DG_CUDA(cudaEventSynchronize(v->ev_read));
-    // the frames before the copy have completed; their error word is read without
-    // clearing it (later frames may still be running), so the next synchronous
-    // call reports it again
-    uint32_t err = 0;
-    DG_CUDA(cudaMemcpyAsync(&err, c->main.d_err, 4, cudaMemcpyDeviceToHost, c->copy_stream));
-    DG_CUDA(cudaStreamSynchronize(c->copy_stream));
+    DG_CUDA(cudaEventSynchronize(v->ev_read));  // waits for this copy only, not for later ones
+    const uint32_t err = v->h_err ? *v->h_err : 0u;
     for (int b = 1; b < 32; b++)
         if (err & (1u << b)) return (dg_status)b;
     return DG_OK;

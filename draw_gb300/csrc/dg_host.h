@@ -99,6 +99,7 @@ struct Canvas {
     // ev_rendered; ev_read marks its end. While read_pending, the next operation
     // that looks the canvas up first makes the context stream wait for ev_read.
     cudaEvent_t ev_rendered = nullptr, ev_read = nullptr;
+    uint32_t* h_err = nullptr;  // pinned: the error word copied with the frame
     bool read_pending = false;
 };
 
