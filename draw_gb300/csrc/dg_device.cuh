@@ -693,8 +693,19 @@ __device__ __forceinline__ uint32_t shade_colour(const DgJobDev& job, const DgTe
                                                  const MatVals& m, float pu, float pv, V3 pn, const float* inv255,
                                                  int& errc, LV lv) {
     const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
-    const DgTexDev& tkd = m.map_kd < nst ? stex[m.map_kd] : job.tex[m.map_kd];
-    const DgTexDev& tka = m.map_ka < nst ? stex[m.map_ka] : job.tex[m.map_ka];
+    // descriptors by value: shared-memory loads for the first DG_SMEM_TEX maps
+    auto tex_desc = [&](uint32_t i) -> DgTexDev {
+        if (i < nst) return stex[i];
+        DgTexDev t;
+        const uint4* g = reinterpret_cast<const uint4*>(job.tex + i);
+        uint4* d = reinterpret_cast<uint4*>(&t);
+        d[0] = __ldg(g);
+        d[1] = __ldg(g + 1);
+        d[2] = __ldg(g + 2);
+        return t;
+    };
+    const DgTexDev tkd = tex_desc(m.map_kd);
+    const DgTexDev tka = m.map_ka == m.map_kd ? tkd : tex_desc(m.map_ka);
     uint32_t kd_rgb = 0, ka_rgb = 0;
     if (!tex_rgb(tkd, pu, pv, kd_rgb)) {
         errc = DG_E_TEXTURE_RANGE;
