@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-plain leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-stress", action="store_true", help="skip the stress leg")
+    ap.add_argument("--no-torus", action="store_true", help="skip the torus leg")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--batch-frames", type=int, default=256)
@@ -432,7 +433,7 @@ def run_ours(args, world, rank, local):
 
     if rank == 0 and world == 1 and not args.no_stress:
         line["stress"] = stress_leg(ctx, stream, flush, peak, cpu=not args.no_cpu)
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not args.no_torus:
         line["torus"] = torus_leg(ctx, stream, flush, peak, cpu=not args.no_cpu)
 
     if rank == 0 and world == 1 and not args.no_cpu:
