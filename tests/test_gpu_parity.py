@@ -184,3 +184,28 @@ def test_clip_deferral_overflow_keeps_results(gpu_ctx, oracle_lib):
             assert gpu_ctx.last_stats()["clip_rows"] > 0
     finally:
         gpu_ctx.set_tuning(**before)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_seeded_random_scenes_and_tunings(seed, gpu_ctx, oracle_lib):
+    """Seeded variations of the micro-sphere field (sphere size, depth slab, screen
+    window, near-plane crossing) rendered under random launch shapes, including a
+    record limit that sends some pixels down the record-less path: every frame
+    equals the oracle's."""
+    rng = np.random.default_rng(1000 + seed)
+    desc = S.micro_sphere_field(width=int(rng.choice([320, 480, 640])), height=int(rng.choice([240, 360])),
+                                n_tris=int(rng.integers(20_000, 150_000)), seed=int(rng.integers(1, 10_000)),
+                                tex=64, n_lights=int(rng.integers(1, 5)), disc_px=float(rng.uniform(1.5, 12.0)),
+                                window=float(rng.uniform(0.2, 1.0)), slab=float(rng.uniform(1.0, 30.0)))
+    ref = oracle_render(desc)
+    knobs = dict(small_max_px=int(rng.choice([0, 4, 16, 64, 256])), item_units=int(rng.choice([1, 4, 8, 32])),
+                 setup_blocks_per_sm=int(rng.choice([1, 4, 16])), queue_blocks_per_sm=int(rng.choice([1, 8, 32])),
+                 tile_rows=int(rng.choice([8, 16, 32])), record_limit=int(rng.choice([0, 0, 2000])))
+    before = gpu_ctx.get_tuning()
+    try:
+        gpu_ctx.set_tuning(**knobs)
+        got = gpu_render(desc, gpu_ctx)
+        p = compare(ref, got, desc.clear_depth)
+        assert p.ok, f"{desc.name} {knobs}: {describe(p)}; {first_mismatch(ref, got)}"
+    finally:
+        gpu_ctx.set_tuning(**before)
