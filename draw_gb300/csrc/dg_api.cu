@@ -294,7 +294,7 @@ Canvas* get_canvas(dg_ctx* c, int32_t id) {
     return v;
 }
 void free_canvas(Canvas& v) {
-    dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
+    dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis); dfree(v.d_cells);
     if (v.ev_rendered) cudaEventDestroy(v.ev_rendered);
     if (v.ev_read) cudaEventDestroy(v.ev_read);
     if (v.h_err) cudaFreeHost(v.h_err);
@@ -321,7 +321,8 @@ dg_status resolve_frames(dg_ctx* c, const int32_t* scenes, const int32_t* canvas
         if (!s || !cv) return DG_E_INVALID;
         if (!cv->depth_init) return DG_E_DEPTH_UNINIT;
         sc[i] = s;
-        tg[i] = FrameTarget{cv->d_colour, cv->d_depth, cv->d_vis, cv->w, cv->h, cv->depth_max, cv->off_x, cv->off_y};
+        tg[i] = FrameTarget{cv->d_colour, cv->d_depth, cv->d_vis,   cv->w,      cv->h,
+                            cv->depth_max, cv->off_x, cv->off_y, cv->d_cells, ++cv->epoch};
     }
     return DG_OK;
 }
@@ -334,11 +335,12 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
     dg_status e = resolve_frames(c, scenes, canvases, n, sc, tg);
     if (e) return e;
     // An object with transparent meshes advances its painter's order once per
-    // render of it; frames that render such an object again start a new job.
+    // render of it, and a canvas holds one frame's visibility keys: frames that
+    // render such an object or a canvas again start a new job.
     uint32_t first = 0;
-    std::vector<int32_t> seen;
+    std::vector<int32_t> seen, seen_canvas;
     for (uint32_t i = 0; i < n; i++) {
-        bool repeat = false;
+        bool repeat = std::find(seen_canvas.begin(), seen_canvas.end(), canvases[i]) != seen_canvas.end();
         for (int32_t oid : sc[i]->objects)
             if (oid >= 0 && (size_t)oid < c->objects.size() && c->objects[oid].nt &&
                 std::find(seen.begin(), seen.end(), oid) != seen.end())
@@ -348,9 +350,11 @@ dg_status render_job(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, 
             if (e) return e;
             first = i;
             seen.clear();
+            seen_canvas.clear();
         }
         for (int32_t oid : sc[i]->objects)
             if (oid >= 0 && (size_t)oid < c->objects.size() && c->objects[oid].nt) seen.push_back(oid);
+        seen_canvas.push_back(canvases[i]);
     }
     return launch_frames(c, c->main, sc.data() + first, tg.data() + first, n - first);
 }
@@ -526,6 +530,8 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         f.width = (uint32_t)tg.w;
         f.height = (uint32_t)tg.h;
         f.vis = tg.vis;
+        f.cells = tg.cells;
+        f.epoch = tg.epoch;
         f.colour = tg.colour;
         f.depth = tg.depth;
         f.seg_begin = (uint32_t)segs.size();
@@ -1198,12 +1204,15 @@ dg_status dg_canvas_create(dg_ctx* c, uint64_t width, uint64_t height, int32_t* 
     if (e) return e;
     Canvas v;
     uint64_t n = width * height;
-    if ((e = dalloc(&v.d_colour, n)) || (e = dalloc(&v.d_depth, n)) || (e = dalloc(&v.d_vis, n))) {
-        dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis);
+    const uint64_t nc = dg_cell_count(width, height);
+    if ((e = dalloc(&v.d_colour, n)) || (e = dalloc(&v.d_depth, n)) || (e = dalloc(&v.d_vis, n)) ||
+        (e = dalloc(&v.d_cells, nc))) {
+        dfree(v.d_colour); dfree(v.d_depth); dfree(v.d_vis); dfree(v.d_cells);
         return e;
     }
     v.w = width;
     v.h = height;
+    DG_CUDA(cudaMemsetAsync(v.d_cells, 0, nc * sizeof(uint32_t), c->main.stream));
     // Canvas::new: black frame (canvas.rs:368), no depth buffer yet
     DG_CUDA(dg_launch_fill(v.d_colour, v.d_depth, n, 0xFF000000u, 0.0f, 1, 0, c->main.stream));
     DG_CUDA(dg_launch_vis_reset(v.d_vis, n, c->main.stream));
@@ -1254,18 +1263,22 @@ dg_status dg_canvas_resize(dg_ctx* c, int32_t id, uint64_t width, uint64_t heigh
     uint32_t* col = nullptr;
     float* dep = nullptr;
     uint64_t* vis = nullptr;
-    if ((e = dalloc(&col, n)) || (e = dalloc(&dep, n)) || (e = dalloc(&vis, n))) {
-        dfree(col); dfree(dep); dfree(vis);
+    uint32_t* cells = nullptr;
+    const uint64_t nc = dg_cell_count(width, height);
+    if ((e = dalloc(&col, n)) || (e = dalloc(&dep, n)) || (e = dalloc(&vis, n)) || (e = dalloc(&cells, nc))) {
+        dfree(col); dfree(dep); dfree(vis); dfree(cells);
         return e;
     }
+    DG_CUDA(cudaMemsetAsync(cells, 0, nc * sizeof(uint32_t), st));
     DG_CUDA(dg_launch_fill(col, dep, n, 0xFF000000u, 0.0f, 1, 0, st));
     DG_CUDA(cudaMemcpyAsync(col, v->d_colour, std::min(n, n_old) * 4, cudaMemcpyDeviceToDevice, st));
     DG_CUDA(dg_launch_vis_reset(vis, n, st));
     DG_CUDA(cudaStreamSynchronize(st));
-    dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis);
+    dfree(v->d_colour); dfree(v->d_depth); dfree(v->d_vis); dfree(v->d_cells);
     v->d_colour = col;
     v->d_depth = dep;
     v->d_vis = vis;
+    v->d_cells = cells;
     v->w = width;
     v->h = height;
     // init_depth(depth_max) (canvas.rs:392)

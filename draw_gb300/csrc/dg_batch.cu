@@ -177,6 +177,13 @@ dg_status time_tuning(dg_ctx* c, const int32_t* scenes, const int32_t* canvases,
     return DG_OK;
 }
 
+// One job renders each canvas at most once (a canvas holds one frame's visibility keys).
+bool canvases_distinct(const int32_t* canvases, uint32_t n) {
+    std::vector<int32_t> v(canvases, canvases + n);
+    std::sort(v.begin(), v.end());
+    return std::adjacent_find(v.begin(), v.end()) == v.end();
+}
+
 }  // namespace
 
 extern "C" {
@@ -184,6 +191,7 @@ extern "C" {
 dg_status dg_batch_create(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n, dg_batch** out) {
     if (!c || !out || n == 0 || !scenes || !canvases) return DG_E_INVALID;
     *out = nullptr;
+    if (!canvases_distinct(canvases, n)) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;
     std::vector<Scene*> sc;
     std::vector<FrameTarget> tg;
@@ -272,6 +280,7 @@ dg_status dg_batch_destroy(dg_batch* b) {
 dg_status dg_autotune(dg_ctx* c, const int32_t* scenes, const int32_t* canvases, uint32_t n, uint32_t reps,
                       dg_tuning* best, float* best_ms) {
     if (!c || n == 0 || !scenes || !canvases || reps == 0 || reps > 1000) return DG_E_INVALID;
+    if (!canvases_distinct(canvases, n)) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;
     dg_status e = set_device(c);
     if (e) return e;

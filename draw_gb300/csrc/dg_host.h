@@ -92,6 +92,8 @@ struct Canvas {
     uint32_t* d_colour = nullptr;
     float* d_depth = nullptr;
     uint64_t* d_vis = nullptr;
+    uint32_t* d_cells = nullptr;  // DgFrameDev::cells; zeroed at allocation
+    uint32_t epoch = 0;           // advanced for every frame rendered into the canvas
     bool depth_init = false;
     float depth_max = 0.0f;
     float off_x = 0.0f, off_y = 0.0f;
@@ -111,7 +113,12 @@ struct FrameTarget {
     uint64_t w, h;
     float clear_depth;
     float off_x, off_y;
+    uint32_t* cells;  // DgFrameDev::cells (or null)
+    uint32_t epoch;   // differs from the frame's other renders into the same cells
 };
+
+// Words of DgFrameDev::cells for a w x h canvas.
+inline uint64_t dg_cell_count(uint64_t w, uint64_t h) { return ((w + 31u) / 32u) * ((h + 31u) / 32u); }
 
 // Scratch, staging and stream of one render job in flight. The context owns
 // one; the render server owns one per concurrent batch.

@@ -74,6 +74,13 @@ struct alignas(16) DgFrameDev {
     uint32_t tile_begin, tiles_x;   // this frame's resolve tiles
     uint32_t pix_begin;             // job-wide index of this frame's first pixel
     uint32_t tt_begin;              // job-wide index of this frame's first transparent triangle
+    uint32_t epoch;                 // this frame's mark in `cells`
+    // One word per 32x32 pixel cell of the canvas, row-major (tiles_x per row):
+    // the setup pass writes `epoch` into every cell that a triangle's bounding
+    // box reaches, so a cell whose word differs from `epoch` got no fragment
+    // this frame and k_resolve writes the clear values there without reading
+    // its keys. Null: every tile takes the full path.
+    uint32_t* cells;
     uint32_t pad[2];
 };
 static_assert(sizeof(DgTexDev) == 48 && sizeof(DgMatDev) == 48, "descriptor sizes");

@@ -14,8 +14,10 @@
 //   k_queue_raster  light/halfway vectors of the marked vertices, then the
 //                   queued triangles' bounding-box pixels in 32-pixel units
 //                   spread evenly over all warps
-//   k_resolve       per 32 x tile_rows tile: empty pixels get the clear colour
-//                   and depth, covered ones are compacted into the tile's
+//   k_resolve       per 32 x tile_rows tile: a tile that no triangle box reached
+//                   (its 32x32 cell lacks the frame's epoch) gets the clear
+//                   values without reading its keys; otherwise empty pixels
+//                   get the clear colour and depth, covered ones are compacted into the tile's
 //                   shade list and their winning fragment is shaded once
 //                   (canvas.rs:682-745, 906-930)
 //
@@ -243,6 +245,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                 uint32_t nu = 0;     // work units to queue (0: not queued)
                 uint32_t qpx = 0;    // bounding-box pixels of the queued triangle
                 bool inplace = false;
+                bool boxed = false;  // the triangle has a box (no NaN centre)
                 tr.xlo = tr.xhi = tr.ylo = tr.yhi = 0;
                 tr.frame = 0;
                 if (has) {
@@ -263,6 +266,7 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                     if (!nan) {  // any NaN centre makes every barycentric NaN: nothing is covered
                         bbox_axis(tr.ax, tr.bx, tr.cx, fr.width, tr.xlo, tr.xhi);
                         bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
+                        boxed = true;
                         make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
                         if (rbase != DG_NONE) {
                             if (!clipped)
@@ -280,6 +284,40 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                             qpx = (uint32_t)px;  // below 2^31: the canvas has fewer pixels
                             nu = (uint32_t)((px + DG_UNIT_PX - 1u) / DG_UNIT_PX);
                         }
+                    }
+                }
+                // Every fragment of a triangle lies in its box: mark the box's 32x32 cells in
+                // the frame's cell map. A box of more than 16 cells is marked by the whole
+                // warp, row by row (a near triangle's box can span the canvas).
+                {
+                    uint32_t* cells = nullptr;
+                    uint32_t ep = 0, cw = 0, ncx = 0, ncy = 0;
+                    if (boxed) {
+                        const DgFrameDev& fm = job.frames[tr.frame];
+                        cells = fm.cells;
+                        ep = fm.epoch;
+                        cw = fm.tiles_x;
+                        if (cells != nullptr) {
+                            ncx = (tr.xhi >> 5) - (tr.xlo >> 5) + 1u;
+                            ncy = (tr.yhi >> 5) - (tr.ylo >> 5) + 1u;
+                        }
+                    }
+                    const uint32_t c0 = (tr.ylo >> 5) * cw + (tr.xlo >> 5), ncell = ncx * ncy;
+                    if (ncell <= 16u) {
+                        for (uint32_t cy = 0; cy < ncy; cy++)
+                            for (uint32_t cx = 0; cx < ncx; cx++) cells[c0 + cy * cw + cx] = ep;
+                    }
+                    unsigned big = __ballot_sync(FULL, ncell > 16u);
+                    while (big) {
+                        const int L = __ffs(big) - 1;
+                        big &= big - 1u;
+                        uint32_t* lc = reinterpret_cast<uint32_t*>(
+                            __shfl_sync(FULL, (unsigned long long)reinterpret_cast<uintptr_t>(cells), L));
+                        const uint32_t ly = __shfl_sync(FULL, ncy, L), lx = __shfl_sync(FULL, ncx, L);
+                        const uint32_t l0 = __shfl_sync(FULL, c0, L), lw = __shfl_sync(FULL, cw, L);
+                        const uint32_t le = __shfl_sync(FULL, ep, L);
+                        for (uint32_t cy = 0; cy < ly; cy++)
+                            for (uint32_t cx = lane; cx < lx; cx += 32u) lc[l0 + cy * lw + cx] = le;
                     }
                 }
                 // Queue this round's large triangles with one 64-bit atomic per warp: it hands out
@@ -624,6 +662,8 @@ __device__ __noinline__ void shade_tile_without_records(const DgJobDev& job, uin
 
 // Resolve and shade, fused: one 32 x TH tile per CTA of 256 threads (TH = 8,
 // 16 or 32: the tile_rows knob).
+//  0. If the tile's 32x32 cell does not hold the frame's epoch, no triangle's
+//     box reached it and every key is empty: the clear values, and return.
 //  1. Each thread reads the visibility keys of TH/8 pixels (rows r, r+8, ...
 //     of its column). An empty pixel gets the clear colour and depth
 //     (this is Canvas::clear, canvas.rs:425-433); a covered one has its key
@@ -656,6 +696,19 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJo
     const uint32_t x = tx * DG_TILE_W + lane;
     const uint32_t W = fr.width, H = fr.height;
     constexpr int R = TH / 8;
+    if (fr.cells != nullptr && __ldcg(fr.cells + ((ty * TH) >> 5) * fr.tiles_x + tx) != fr.epoch) {
+        // No triangle's box reached the tile's 32x32 cell this frame, so all its
+        // keys are empty: the clear values, without reading the keys (block-uniform).
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            const uint32_t y = ty * TH + wid + 8u * j;
+            if (x < W && y < H) {
+                fr.depth[(uint64_t)y * W + x] = fr.clear_depth;
+                fr.colour[(uint64_t)(H - 1u - y) * W + x] = AZUL_BB;
+            }
+        }
+        return;
+    }
     uint64_t key[R];
 #pragma unroll
     for (int j = 0; j < R; j++) {  // all loads first: R keys in flight per thread

@@ -39,7 +39,7 @@ struct Request {
     uint64_t ticket = 0;
     Scene scene;
     FrameTarget tgt{};
-    void* mem = nullptr;  // one allocation: colour | depth | vis
+    void* mem = nullptr;  // one allocation: vis | colour | depth | cells
     uint64_t bytes = 0;
     double t_submit = 0, t_start = 0, t_done = 0;
     int state = kPending;
@@ -82,7 +82,7 @@ struct dg_server {
 
 namespace {
 
-uint64_t request_bytes(uint64_t w, uint64_t h) { return w * h * (4 + 4 + 8); }
+uint64_t request_bytes(uint64_t w, uint64_t h) { return w * h * (4 + 4 + 8) + dg_cell_count(w, h) * 4; }
 
 // Host callback at the end of a batch on its slot stream (no CUDA calls allowed here).
 void CUDART_CB batch_done(void* arg) {
@@ -138,6 +138,10 @@ dg_status launch_batch(dg_server* s, Slot* sl, std::vector<Request*>& batch, uin
         r->tgt.vis = reinterpret_cast<uint64_t*>(base);
         r->tgt.colour = reinterpret_cast<uint32_t*>(base + n * 8);
         r->tgt.depth = reinterpret_cast<float*>(base + n * 12);
+        // the cells keep whatever the memory held: a word equal to this request's
+        // ticket (unique among the server's requests) was written by this frame
+        r->tgt.cells = reinterpret_cast<uint32_t*>(base + n * 16);
+        r->tgt.epoch = (uint32_t)r->ticket;
         r->tgt.w = r->scene.width;
         r->tgt.h = r->scene.height;
         r->tgt.off_x = r->tgt.off_y = 0.0f;

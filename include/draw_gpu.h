@@ -239,7 +239,8 @@ dg_status dg_canvas_size(dg_ctx* ctx, int32_t canvas, uint64_t* width, uint64_t*
  * stream; results are bit-identical to the reference's serial loop. */
 dg_status dg_scene_render(dg_ctx* ctx, int32_t scene, int32_t canvas);
 /* Renders n independent (scene, canvas) frames with one launch per pipeline
- * stage (the batched form). Equivalent to n dg_scene_render calls. */
+ * stage (the batched form). Equivalent to n dg_scene_render calls: a canvas
+ * that appears again starts a new job, so the later frame overwrites it. */
 dg_status dg_render_batch(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n);
 
 /* ---------------------------------------------------- graph-replayed batch
@@ -252,8 +253,9 @@ dg_status dg_render_batch(dg_ctx* ctx, const int32_t* scenes, const int32_t* can
  * host rewrites the uploaded descriptors); a change of shape (objects added to
  * a scene, a canvas resized or destroyed, texture maps added, dg_ctx_set_tuning)
  * is detected and re-captured at the next dg_batch_render. Each replay renders
- * exactly what n dg_scene_render calls would. The batch holds its own scratch
- * memory; kernel errors surface at the context's next synchronizing call. */
+ * exactly what n dg_scene_render calls would. The n canvases must be distinct
+ * (DG_E_INVALID otherwise). The batch holds its own scratch memory; kernel
+ * errors surface at the context's next synchronizing call. */
 typedef struct dg_batch dg_batch;
 dg_status dg_batch_create(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n, dg_batch** out);
 dg_status dg_batch_render(dg_batch* b);
@@ -265,7 +267,8 @@ dg_status dg_batch_destroy(dg_batch* b);
  * caller's frames (two sweeps; each candidate timed with CUDA events over
  * `reps` renders of the n frames after one warm-up render). Sets the fastest
  * tuning on ctx and returns it with its time per render in best_ms (either
- * pointer may be NULL). The knobs do not change what is rendered. */
+ * pointer may be NULL). The knobs do not change what is rendered. The n
+ * canvases must be distinct (DG_E_INVALID otherwise). */
 dg_status dg_autotune(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvases, uint32_t n, uint32_t reps,
                       dg_tuning* best, float* best_ms);
 
@@ -275,7 +278,8 @@ dg_status dg_autotune(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvase
  * render requests from any thread as they arrive, keeps meshes and textures
  * resident (objects of the context), admits requests in arrival order against
  * a device-memory budget (each request holds W*H*16 bytes of colour, depth and
- * visibility buffers; job scratch counts too), packs up to max_batch admitted
+ * visibility buffers and 4 bytes per 32x32 pixel cell; job scratch counts too),
+ * packs up to max_batch admitted
  * requests into one batched render job, and keeps up to `streams` jobs in flight
  * on separate streams. Each request renders exactly as dg_scene_render would
  * render it alone. While a server runs, its context must not be modified or

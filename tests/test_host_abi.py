@@ -143,6 +143,11 @@ def test_host_only_context_refuses_device_work(lib):
     n = ctypes.c_uint64()
     assert lib.dg_check_division(h, 1, 16, 1, ctypes.byref(n), None, None) == 6
     assert lib.dg_check_division(h, 4, 16, 1, ctypes.byref(n), None, None) == 1  # no such sample family
+    # a graph batch or an autotune run renders each canvas once: a repeated canvas is refused
+    ids = (ctypes.c_int32 * 2)(0, 0)
+    bp = ctypes.c_void_p()
+    assert lib.dg_batch_create(h, ids, ids, 2, ctypes.byref(bp)) == 1
+    assert lib.dg_autotune(h, ids, ids, 2, 1, None, None) == 1
     lib.dg_ctx_destroy(h)
 
 
