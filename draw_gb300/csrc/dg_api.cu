@@ -399,6 +399,9 @@ void slot_free(JobSlot& s) {
     dfree(s.d_surv);
     dfree(s.d_rec_of);
     dfree(s.d_trec);
+    dfree(s.d_trec_w);
+    dfree(s.d_ttrec_w);
+    s.trec_w_cap = s.ttrec_w_cap = 0;
     dfree(s.d_counters);
     dfree(s.d_err);
     for (int i = 0; i < JobSlot::kStage; i++) {
@@ -438,7 +441,8 @@ dg_status sync_tex_table(dg_ctx* c, cudaStream_t stream) {
         t[i].fw = (float)c->tex[i].w;
         t[i].fh = (float)c->tex[i].h;
         t[i].small = dg_tex_small(c->tex[i].len, c->tex[i].w, c->tex[i].h);
-        t[i].pad[0] = t[i].pad[1] = 0;
+        t[i].filter = c->tex[i].filter;
+        t[i].pad = 0;
     }
     DG_CUDA(cudaStreamSynchronize(stream));
     if (c->d_tex_cap < t.size()) {
@@ -494,6 +498,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0, total_px = 0;
     uint64_t ntt = 0, tmesh_total = 0, max_frame_tt = 0;
     uint32_t stride = 1;
+    bool any_persp = false;
     B.transparent_objects.clear();
     for (uint32_t i = 0; i < n; i++) {
         Scene& s = *scenes[i];  // frame_setup updates the camera basis, as Scene::render does
@@ -525,6 +530,8 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         }
         stride = std::max(stride, f.nlights);
         f.exponent = s.exponent;
+        f.flags = s.interpolation == DG_INTERP_PERSPECTIVE ? DG_FRAME_PERSPECTIVE : 0u;
+        any_persp = any_persp || f.flags != 0u;
         f.off_x = tg.off_x;
         f.off_y = tg.off_y;
         f.width = (uint32_t)tg.w;
@@ -644,6 +651,14 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     if (e) return e;
     e = grow(S, &S.d_trec, &S.trec_cap, trec_records(total_tri));
     if (e) return e;
+    if (any_persp) {
+        e = grow(S, &S.d_trec_w, &S.trec_w_cap, S.trec_cap);
+        if (e) return e;
+        if (ntt) {
+            e = grow(S, &S.d_ttrec_w, &S.ttrec_w_cap, 4 * ntt);
+            if (e) return e;
+        }
+    }
     const size_t want_mark = std::max<uint64_t>(total_vtx, 1);
     if (S.vmark_cap < want_mark) {
         e = grow(S, &S.d_vmark, &S.vmark_cap, want_mark);
@@ -680,6 +695,8 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.surv = S.d_surv;
     job.rec_of = S.d_rec_of;
     job.trec = S.d_trec;
+    job.trec_w = any_persp ? S.d_trec_w : nullptr;
+    job.ttrec_w = any_persp && ntt ? S.d_ttrec_w : nullptr;
     job.trec_cap = (uint32_t)std::min<size_t>(S.trec_cap, 0xFFFFFFF0ull);
     if (S.record_limit) job.trec_cap = std::min(job.trec_cap, S.record_limit);
     job.queue = S.d_queue;
@@ -1152,6 +1169,24 @@ dg_status dg_scene_set_lights(dg_ctx* c, int32_t scene, const float* pos, uint32
     if (!s || !pos || n == 0 || n > DG_MAX_LIGHTS) return DG_E_INVALID;
     s->lights.clear();
     for (uint32_t i = 0; i < n; i++) s->lights.push_back(h3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    return DG_OK;
+}
+
+dg_status dg_scene_set_interpolation(dg_ctx* c, int32_t scene, int32_t mode) {
+    Scene* s = get_scene(c, scene);
+    if (!s || (mode != DG_INTERP_AFFINE && mode != DG_INTERP_PERSPECTIVE)) return DG_E_INVALID;
+    s->interpolation = mode;
+    return DG_OK;
+}
+
+dg_status dg_texmap_set_filter(dg_ctx* c, int32_t texmap, int32_t filter) {
+    if (!c || texmap < 0 || (size_t)texmap + 1 >= c->tex.size() ||
+        (filter != DG_FILTER_NEAREST && filter != DG_FILTER_BILINEAR))
+        return DG_E_INVALID;
+    if (c->tex[(size_t)texmap + 1].filter != (uint32_t)filter) {
+        c->tex[(size_t)texmap + 1].filter = (uint32_t)filter;
+        c->tex_dirty = true;
+    }
     return DG_OK;
 }
 

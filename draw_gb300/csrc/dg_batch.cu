@@ -75,6 +75,7 @@ void signature(const dg_batch* b, const std::vector<Scene*>& sc, const std::vect
         sig.push_back(tg[i].w);
         sig.push_back(tg[i].h);
         sig.push_back(sc[i]->lights.size());
+        sig.push_back((uint64_t)(uint32_t)sc[i]->interpolation);
         sig.push_back(sc[i]->objects.size());
         for (int32_t oid : sc[i]->objects) {
             sig.push_back((uint64_t)(uint32_t)oid);

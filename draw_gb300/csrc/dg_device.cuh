@@ -122,6 +122,27 @@ __device__ __forceinline__ void project_snap(const DgFrameDev& fr, V3 p, float& 
     cy = floorf(fA(sy, 0.5f));
 }
 
+// The clip-space w of world position p: the fourth row of M * (p, 1), the
+// divisor of the projection above (scene/mod.rs:1047-1050).
+__device__ __forceinline__ float proj_w(const DgFrameDev& fr, V3 p) {
+    return fA(fA(fA(fA(0.0f, fM(fr.M[3][0], p.x)), fM(fr.M[3][1], p.y)), fM(fr.M[3][2], p.z)), fM(fr.M[3][3], 1.0f));
+}
+
+// Extension (no counterpart in the reference): perspective-correct weights.
+// From the reference's screen-space barycentrics and iw = (1/w_a, 1/w_b, 1/w_c):
+// pa = alpha * iw_a, pb = beta * iw_b, pc = gama * iw_c, s = (pa + pb) + pc,
+// and the weights become pa / s, pb / s, pc / s.
+__device__ __forceinline__ void persp_weights(float& al, float& be, float& ga, float4 iw) {
+    const float pa = fM(al, iw.x), pb = fM(be, iw.y), pc = fM(ga, iw.z);
+    const float s = fA(fA(pa, pb), pc);
+    al = fD(pa, s);
+    be = fD(pb, s);
+    ga = fD(pc, s);
+}
+__device__ __forceinline__ float4 inv_w3(const DgFrameDev& fr, V3 a, V3 b, V3 c) {
+    return make_float4(fD(1.0f, proj_w(fr, a)), fD(1.0f, proj_w(fr, b)), fD(1.0f, proj_w(fr, c)), 0.0f);
+}
+
 // A vertex as the raster setup uses it: snapped screen centre, eye distance
 // (scene/mod.rs:924) and the plane-sign mask of k_vertex, for a job vertex at
 // world position p.
@@ -515,9 +536,16 @@ __device__ __forceinline__ void mat_words(const DgSegDev& sg, uint32_t mi, float
 }
 
 // Triangle record of an unclipped triangle (its vertices are the mesh's).
+// Wout (frames with DG_FRAME_PERSPECTIVE, else null): receives inv_w3 of the
+// triangle's vertices.
 __device__ __forceinline__ void write_record(const DgJobDev& job, DgTriRec* R, const DgSegDev& sg, uint4 tp, uint4 tuv,
-                                             uint4 tnr, const EdgeSet& e, const float4 r[3]) {
+                                             uint4 tnr, const EdgeSet& e, const float4 r[3], const DgFrameDev& fr,
+                                             float4* Wout) {
     store_edges(R, e);
+    if (Wout) {
+        const float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
+        *Wout = inv_w3(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z});
+    }
     const float2 u0 = __ldg(sg.uv + tuv.x), u1 = __ldg(sg.uv + tuv.y), u2 = __ldg(sg.uv + tuv.z);
     const float4 n0 = __ldg(sg.nrm + tnr.x), n1 = __ldg(sg.nrm + tnr.y), n2 = __ldg(sg.nrm + tnr.z);
     float mw[9];
@@ -539,8 +567,10 @@ __device__ __forceinline__ void write_record(const DgJobDev& job, DgTriRec* R, c
 // the light/halfway rows of new vertex k are rowbase + (k - 3).
 __device__ __noinline__ void write_clip_record(const DgJobDev& job, DgTriRec* R, const DgSegDev& sg, uint4 tp,
                                                uint4 tuv, uint4 tnr, const EdgeSet& e, const RTri& tr,
-                                               const ClipProg& P, int o, uint32_t rowbase) {
+                                               const ClipProg& P, int o, uint32_t rowbase, const DgFrameDev& fr,
+                                               float4* Wout) {
     store_edges(R, e);
+    if (Wout) *Wout = inv_w3(fr, P.pos[P.out[o][0]], P.pos[P.out[o][1]], P.pos[P.out[o][2]]);
     const float2 u0 = __ldg(sg.uv + tuv.x), u1 = __ldg(sg.uv + tuv.y), u2 = __ldg(sg.uv + tuv.z);
     const float4 n0 = __ldg(sg.nrm + tnr.x), n1 = __ldg(sg.nrm + tnr.y), n2 = __ldg(sg.nrm + tnr.z);
     float mw[9];
@@ -675,6 +705,51 @@ __device__ __forceinline__ bool tex_rgb(const DgTexDev& tx, float u, float v, ui
     return true;
 }
 
+// Three image bytes at byte offset off (off <= len - 3) as the low 24 bits.
+__device__ __forceinline__ uint32_t tex_bytes3(const DgTexDev& tx, uint64_t off) {
+    const uint64_t w = off >> 2;
+    const uint32_t sh = (uint32_t)(off & 3ull) * 8u;
+    const uint32_t lo = __ldg(tx.words + w);
+    return sh <= 8u ? (lo >> sh) : __funnelshift_r(lo, __ldg(tx.words + w + 1), sh);
+}
+
+// Extension (no counterpart in the reference, which samples the nearest texel):
+// bilinear fetch. x = u * (W - 1), y = v * (H - 1) as in get_rgb_slice; the base
+// texel (floor x, floor y) has the nearest texel's wrapping offset; its
+// neighbours are the next column (when it exists, else the same column) and the
+// next row up (the previous row in memory, when it exists, else the same row).
+// Per channel, with c = byte / 255, ax = x - floor x, ay = y - floor y:
+// t0 = c00 (1 - ax) + c01 ax, t1 = c10 (1 - ax) + c11 ax, c = t0 (1 - ay) + t1 ay.
+// False (the texture-range error) when any of the four offsets is past the image.
+__device__ __noinline__ bool tex_bilinear(const DgTexDev& tx, float u, float v, const float* inv255, V3& out) {
+    const float x = fM(u, fS(tx.fw, 1.0f)), y = fM(v, fS(tx.fh, 1.0f));
+    const float fx = floorf(x), fy = floorf(y);
+    const float ax = fS(x, fx), ay = fS(y, fy);
+    const uint64_t ui = as_usize(fx);
+    const uint64_t vi = (uint64_t)tx.height - 1ull - as_usize(fy);
+    const uint64_t o00 = (vi * (uint64_t)tx.width + ui) * (uint64_t)tx.comps;
+    const uint64_t dx = (ui + 1ull < (uint64_t)tx.width) ? (uint64_t)tx.comps : 0ull;
+    const uint64_t dy = (vi >= 1ull && vi < (uint64_t)tx.height) ? (uint64_t)tx.width * tx.comps : 0ull;
+    const uint64_t off[4] = {o00, o00 + dx, o00 - dy, o00 - dy + dx};
+    uint32_t c[4];
+    for (int k = 0; k < 4; k++) {
+        if (tx.len < 3ull || off[k] > tx.len - 3ull) return false;
+        c[k] = tex_bytes3(tx, off[k]);
+    }
+    const float bx = fS(1.0f, ax), by = fS(1.0f, ay);
+    float ch[3];
+    for (int i = 0; i < 3; i++) {
+        const uint32_t sh = 8u * (uint32_t)i;
+        const float c00 = inv255[(c[0] >> sh) & 0xFFu], c01 = inv255[(c[1] >> sh) & 0xFFu];
+        const float c10 = inv255[(c[2] >> sh) & 0xFFu], c11 = inv255[(c[3] >> sh) & 0xFFu];
+        const float t0 = fA(fM(c00, bx), fM(c01, ax));
+        const float t1 = fA(fM(c10, bx), fM(c11, ax));
+        ch[i] = fA(fM(t0, by), fM(t1, ay));
+    }
+    out = V3{ch[0], ch[1], ch[2]};
+    return true;
+}
+
 // A triangle's material as the shading formula uses it.
 struct MatVals {
     V3 ka, kd, ks;
@@ -706,21 +781,26 @@ __device__ __forceinline__ uint32_t shade_colour(const DgJobDev& job, const DgTe
     };
     const DgTexDev tkd = tex_desc(m.map_kd);
     const DgTexDev tka = m.map_ka == m.map_kd ? tkd : tex_desc(m.map_ka);
-    uint32_t kd_rgb = 0, ka_rgb = 0;
-    if (!tex_rgb(tkd, pu, pv, kd_rgb)) {
+    // Pixel::normalized_as_vec3 (canvas.rs:81-87): byte / 255.0, looked up in a
+    // table of the 256 correctly rounded quotients; or the bilinear extension
+    auto sample = [&](const DgTexDev& t, V3& out) -> bool {
+        if (t.filter == DG_FILTER_BILINEAR) return tex_bilinear(t, pu, pv, inv255, out);
+        uint32_t rgb = 0;
+        if (!tex_rgb(t, pu, pv, rgb)) return false;
+        out = V3{inv255[rgb & 0xFFu], inv255[(rgb >> 8) & 0xFFu], inv255[(rgb >> 16) & 0xFFu]};
+        return true;
+    };
+    V3 diffuse, ambient;
+    if (!sample(tkd, diffuse)) {
         errc = DG_E_TEXTURE_RANGE;
         return 0u;
     }
     if (m.map_ka == m.map_kd) {
-        ka_rgb = kd_rgb;  // the same map at the same coordinates
-    } else if (!tex_rgb(tka, pu, pv, ka_rgb)) {
+        ambient = diffuse;  // the same map at the same coordinates
+    } else if (!sample(tka, ambient)) {
         errc = DG_E_TEXTURE_RANGE;
         return 0u;
     }
-    // Pixel::normalized_as_vec3 (canvas.rs:81-87): byte / 255.0, looked up in a
-    // table of the 256 correctly rounded quotients
-    const V3 diffuse = {inv255[kd_rgb & 0xFFu], inv255[(kd_rgb >> 8) & 0xFFu], inv255[(kd_rgb >> 16) & 0xFFu]};
-    const V3 ambient = {inv255[ka_rgb & 0xFFu], inv255[(ka_rgb >> 8) & 0xFFu], inv255[(ka_rgb >> 16) & 0xFFu]};
     const V3 c_l = m.ks;
     const V3 c_r = {fM(diffuse.x, m.kd.x), fM(diffuse.y, m.kd.y), fM(diffuse.z, m.kd.z)};
     const V3 c_a = {fM(ambient.x, m.ka.x), fM(ambient.y, m.ka.y), fM(ambient.z, m.ka.z)};
@@ -758,9 +838,11 @@ __device__ __forceinline__ const float4* shade_row(const DgJobDev& job, uint32_t
 
 // Shades the winning fragment of pixel (x, y) from its triangle record:
 // canvas.rs:682-741.
+// Wp (frames with DG_FRAME_PERSPECTIVE, else null): the record's inv_w3.
 __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const DgFrameDev& fr, const DgTriRec* R,
                                                       uint32_t x, uint32_t y, const float* inv255,
-                                                      const DgTexDev* stex, float& depth_out, int& errc) {
+                                                      const DgTexDev* stex, float& depth_out, int& errc,
+                                                      const float4* Wp) {
     errc = DG_OK;
     EdgeSet e;
     load_edges(R, e);
@@ -770,10 +852,11 @@ __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const
     const uint4 rows = __ldg(reinterpret_cast<const uint4*>(R) + 10);
     const uint4 last = __ldg(reinterpret_cast<const uint4*>(R) + 11);
     const float xf = (float)x, yf = (float)y;
-    const float al = fD(edge_eval(e, 0, xf, yf), e.den[0]);
-    const float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
-    const float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
+    float al = fD(edge_eval(e, 0, xf, yf), e.den[0]);
+    float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
+    float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
     depth_out = interp(al, be, ga, dd.x, dd.y, dd.z);
+    if (Wp) persp_weights(al, be, ga, __ldg(Wp));  // coverage and depth keep the screen-space weights
     const float pu = interp(al, be, ga, fu.x, fu.y, fu.z);
     const float pv = interp(al, be, ga, fv.x, fv.y, fv.z);
     const V3 pn = {interp(al, be, ga, fx.x, fx.y, fx.z), interp(al, be, ga, fy.x, fy.y, fy.z),
@@ -845,10 +928,20 @@ __device__ __noinline__ uint32_t shade_without_record(const DgJobDev& job, const
     EdgeSet e;
     make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
     const float xf = (float)x, yf = (float)y;
-    const float al = fD(edge_eval(e, 0, xf, yf), e.den[0]);
-    const float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
-    const float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
+    float al = fD(edge_eval(e, 0, xf, yf), e.den[0]);
+    float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
+    float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
     depth_out = interp(al, be, ga, tr.da, tr.db, tr.dc);
+    if (fr.flags & DG_FRAME_PERSPECTIVE) {
+        float4 iw;
+        if (!clipped) {
+            const float4 pa = __ldg(sg.pos + vi[0]), pb = __ldg(sg.pos + vi[1]), pc = __ldg(sg.pos + vi[2]);
+            iw = inv_w3(fr, V3{pa.x, pa.y, pa.z}, V3{pb.x, pb.y, pb.z}, V3{pc.x, pc.y, pc.z});
+        } else {
+            iw = inv_w3(fr, P.pos[P.out[o][0]], P.pos[P.out[o][1]], P.pos[P.out[o][2]]);
+        }
+        persp_weights(al, be, ga, iw);
+    }
 
     // per-vertex field values of the output triangle
     auto field = [&](float f0, float f1, float f2) -> float {

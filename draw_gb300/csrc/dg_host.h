@@ -49,6 +49,7 @@ struct Scene {  // scene/mod.rs:749-757
     std::vector<int32_t> objects;
     std::vector<HV3> lights;
     int32_t exponent = 2;
+    int32_t interpolation = DG_INTERP_AFFINE;  // extension (dg_scene_set_interpolation)
 };
 
 dg_status camera_init(Camera& c, HV3 pos, HV3 dir, float ratio, float near_, float far_, float fov_x);
@@ -62,6 +63,7 @@ struct TexMap {
     uint32_t* d_words = nullptr;
     uint64_t len = 0;
     uint32_t w = 0, h = 0, comps = 0;
+    uint32_t filter = DG_FILTER_NEAREST;  // extension (dg_texmap_set_filter)
 };
 
 struct Object {
@@ -160,6 +162,10 @@ struct JobSlot {
     size_t rec_of_cap = 0;
     DgTriRec* d_trec = nullptr;
     size_t trec_cap = 0;
+    float4* d_trec_w = nullptr;  // perspective weights per record (grown only for perspective frames)
+    size_t trec_w_cap = 0;
+    float4* d_ttrec_w = nullptr;  // the same for the transparent records
+    size_t ttrec_w_cap = 0;
     uint32_t small_max_px = DG_SMALL_MAX_PX;  // dg_tuning knobs
     uint32_t setup_blocks_per_sm = DG_SETUP_BLOCKS_PER_SM;
     uint32_t queue_blocks_per_sm = DG_QUEUE_BLOCKS_PER_SM;

@@ -47,7 +47,8 @@ struct alignas(16) DgTexDev {
     uint32_t width, height, comps;
     float fw, fh;           // width as f32, height as f32
     uint32_t small;         // 1 if len < 2^32 and width, height < 2^24 (32-bit texel offsets suffice)
-    uint32_t pad[2];
+    uint32_t filter;        // DG_FILTER_NEAREST (the reference) or DG_FILTER_BILINEAR (extension)
+    uint32_t pad;
 };
 
 struct alignas(16) DgMatDev {
@@ -81,8 +82,10 @@ struct alignas(16) DgFrameDev {
     // this frame and k_resolve writes the clear values there without reading
     // its keys. Null: every tile takes the full path.
     uint32_t* cells;
-    uint32_t pad[2];
+    uint32_t flags;  // DG_FRAME_PERSPECTIVE: perspective-correct shading attributes (extension)
+    uint32_t pad;
 };
+#define DG_FRAME_PERSPECTIVE 1u
 static_assert(sizeof(DgTexDev) == 48 && sizeof(DgMatDev) == 48, "descriptor sizes");
 inline uint32_t dg_tex_small(uint64_t len, uint64_t w, uint64_t h) {
     return (len < (1ull << 32) && w < (1ull << 24) && h < (1ull << 24)) ? 1u : 0u;
@@ -196,6 +199,11 @@ struct DgJobDev {
     uint32_t* surv;         // [total_tri] job-wide indices of the triangles that passed the cull pass
     uint32_t* rec_of;       // [total_tri] first DgTriRec of each surviving triangle, or DG_NONE
     DgTriRec* trec;
+    // Per triangle record, (1/w_a, 1/w_b, 1/w_c, 0) of its three vertices' clip
+    // w: written and read only for frames with DG_FRAME_PERSPECTIVE (null when
+    // no frame of the job has it). ttrec_w: the same for ttrec.
+    float4* trec_w;
+    float4* ttrec_w;
     uint32_t trec_cap;
     uint32_t queue_cap;
     DgQueueRec* queue;

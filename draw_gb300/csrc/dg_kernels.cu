@@ -36,8 +36,10 @@
 namespace {
 
 // ================================================================ kernels
-__global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
-    allow_next_kernel();
+// Each pass is a device function over the whole grid (grid-stride or
+// block-uniform loops) wrapped by its kernel; the five kernels run as a chain
+// with programmatic dependent launch.
+__device__ __forceinline__ void dev_vertex(const DgJobDev& job) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < job.total_vtx; v += stride) {
         uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
@@ -57,6 +59,11 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
     }
 }
 
+__global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
+    allow_next_kernel();
+    dev_vertex(job);
+}
+
 
 // Cull pass: one thread per input triangle. A triangle is dropped when one
 // lateral plane has all three vertices at f <= 0 (Triangle::clip_against_planes,
@@ -66,10 +73,9 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
 // the triangle, so testing them in this order gives the reference's surviving
 // set; the plane tests read only the vertex records' sign masks. Survivors are
 // appended (in any order: the visibility key carries the submission index).
-__global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
+__device__ __forceinline__ void dev_cull(const DgJobDev& job) {
     __shared__ uint32_t s_warp[8];
     __shared__ unsigned long long s_base;
-    wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
     // block-uniform loop: survivors are appended with one atomic per block
@@ -112,6 +118,11 @@ __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
+    wait_previous_kernel();
+    dev_cull(job);
+}
+
 
 // Setup pass over the cull survivors (dense, one per thread): near/far
 // clipping, triangle records, bounding boxes and edge functions; tiny
@@ -136,7 +147,7 @@ __device__ __forceinline__ unsigned long long warp_alloc(unsigned long long* c, 
     return old + (incl - n);
 }
 
-__global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
+__device__ __forceinline__ void dev_setup(const DgJobDev& job) {
     __shared__ uint32_t s_records;  // statistics: record requests of the block
     __shared__ uint32_t s_nclip;    // clipped survivors the block deferred
     __shared__ uint32_t s_clip_i[DG_CLIP_DEFER], s_clip_g[DG_CLIP_DEFER];  // their survivor slots and indices
@@ -145,7 +156,6 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
         s_nclip = 0u;
     }
     __syncthreads();
-    wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long ns64 = __ldcg(job.cnt + DG_CNT_SURV);
     const uint32_t nsurv = (uint32_t)(ns64 < job.total_tri ? ns64 : job.total_tri);
@@ -269,11 +279,14 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
                         boxed = true;
                         make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
                         if (rbase != DG_NONE) {
+                            float4* wout = (fr.flags & DG_FRAME_PERSPECTIVE) && job.trec_w
+                                               ? job.trec_w + rbase + (uint32_t)rr
+                                               : nullptr;
                             if (!clipped)
-                                write_record(job, job.trec + rbase, sg, tp, tuv, tnr, e, r);
+                                write_record(job, job.trec + rbase, sg, tp, tuv, tnr, e, r, fr, wout);
                             else
                                 write_clip_record(job, job.trec + rbase + (uint32_t)rr, sg, tp, tuv, tnr, e, tr, P, rr,
-                                                  job.total_vtx + row0);
+                                                  job.total_vtx + row0, fr, wout);
                         }
                         uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
                         if (rbase == DG_NONE) {
@@ -432,6 +445,11 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
     if (threadIdx.x == 0 && s_records) atomicAdd(job.cnt + DG_CNT_TREC, (unsigned long long)s_records);  // statistics only
 }
 
+__global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
+    wait_previous_kernel();
+    dev_setup(job);
+}
+
 // The raster queue: the bounding-box pixels of every queued triangle in
 // row-major units of DG_UNIT_PX (one pixel per lane), grouped into work items
 // of at most job.item_units units that the warps take in a strided order.
@@ -466,11 +484,10 @@ __device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uin
     }
 }
 
-__global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
+__device__ __forceinline__ void dev_queue(const DgJobDev& job) {
     __shared__ uint32_t s_bx[8][64], s_by[8][64];  // per-warp candidate buffers
     __shared__ uint32_t s_sorted[256];             // a group of small triangles in box-size order
     __shared__ uint32_t s_bucket[16];              // their counts, then offsets, per box-size class
-    wait_previous_kernel();
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t* bx = s_bx[threadIdx.x >> 5];
     uint32_t* by = s_by[threadIdx.x >> 5];
@@ -622,6 +639,11 @@ __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
     }
 }
 
+__global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
+    wait_previous_kernel();
+    dev_queue(job);
+}
+
 // Pixels of tile `tile` whose winning triangle has no record (the record
 // buffers were full) kept their keys in phase 1: they are shaded here from the
 // mesh (shade_without_record) and their keys reset. The tile's own CTA calls it
@@ -674,21 +696,24 @@ __device__ __noinline__ void shade_tile_without_records(const DgJobDev& job, uin
 //     pixel is shaded once (canvas.rs:682-741) and its colour (row H-1-y) and
 //     depth (y*W+x) are written (canvas.rs:923-930).
 //  3. If a pixel of the tile had no record, shade_tile_without_records.
-template <uint32_t TH>
-__global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
-    __shared__ float inv255[256];
-    __shared__ DgTexDev stex[DG_SMEM_TEX];
-    __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
-    __shared__ uint32_t s_val[DG_TILE_W * TH];  // triangle record
-    __shared__ uint32_t s_row[33];  // shade-list offset of each tile row; [32] = total
-    // independent of the previous kernel: the quotient table and the texture descriptors
+// The resolve pass's tables, independent of the previous passes: the 256
+// quotients byte / 255 and the first DG_SMEM_TEX texture descriptors.
+__device__ __forceinline__ void resolve_prologue(const DgJobDev& job, float* inv255, DgTexDev* stex) {
     inv255[threadIdx.x] = fD((float)threadIdx.x, 255.0f);
     const uint32_t nst = job.ntex < DG_SMEM_TEX ? job.ntex : DG_SMEM_TEX;
     for (uint32_t i = threadIdx.x; i < nst * 3u; i += blockDim.x)
         reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
-    wait_previous_kernel();
+}
+
+// One tile of the resolve pass (block-uniform; the tables of resolve_prologue
+// must be in place).
+template <uint32_t TH>
+__device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint32_t tile, const float* inv255,
+                                                 const DgTexDev* stex) {
+    __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
+    __shared__ uint32_t s_val[DG_TILE_W * TH];  // triangle record
+    __shared__ uint32_t s_row[33];  // shade-list offset of each tile row; [32] = total
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
-    const uint32_t tile = blockIdx.x;
     const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
     const DgFrameDev& fr = job.frames[fi];
     const uint32_t lt = tile - fr.tile_begin;
@@ -782,7 +807,8 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJo
         const uint32_t px = tx * DG_TILE_W + (pe & 31u), py = ty * TH + (pe >> 5);
         float d = 0.0f;
         int errc;
-        uint32_t c = shade_from_record(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc);
+        const float4* wp = (fr.flags & DG_FRAME_PERSPECTIVE) && job.trec_w ? job.trec_w + s_val[k] : nullptr;
+        uint32_t c = shade_from_record(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc, wp);
         if (errc != DG_OK) c = AZUL_BB;
         // one error-word update per warp (every pixel of a bad job may fail)
         const unsigned act = __activemask();
@@ -793,6 +819,15 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJo
     }
     // pixels whose triangle has no record: shaded the long way (block-uniform)
     if (any_no_record) shade_tile_without_records<TH>(job, tile, inv255, stex);
+}
+
+template <uint32_t TH>
+__global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
+    __shared__ float inv255[256];
+    __shared__ DgTexDev stex[DG_SMEM_TEX];
+    resolve_prologue(job, inv255, stex);
+    wait_previous_kernel();
+    dev_resolve_tile<TH>(job, blockIdx.x, inv255, stex);
 }
 
 __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, float dv, int fc, int fd) {

@@ -10,6 +10,10 @@
 // The scratch is shared by every call and keeps the last call's contents, so
 // each call first resets what must start empty (visibility keys, vertex marks,
 // counters, the error word). Calls whose GPU work overlaps race on it.
+//
+// The job descriptor travels as a kernel parameter: k_noalloc_begin, the first
+// kernel of every call, writes it into the scratch array together with those
+// resets, so no host buffer has to outlive the call.
 #include <cstring>
 #include <mutex>
 
@@ -74,6 +78,27 @@ dg_status scratch_on_current_device(unsigned char** out) {
     }
     *out = g_scratch_ptr[dev];
     return DG_OK;
+}
+
+// Writes the call's job descriptor into the scratch array and resets what the
+// previous call left behind: counters, error word, vertex marks, the 1x1 white
+// default map's texel word, and the visibility keys of npx pixels.
+__global__ void k_noalloc_begin(const __grid_constant__ NoallocDesc d, unsigned char* base, uint32_t npx) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+    static_assert(sizeof(NoallocDesc) % 16 == 0 && kOffDesc % 16 == 0, "descriptor copied in 16-byte words");
+    const uint4* src = reinterpret_cast<const uint4*>(&d);
+    uint4* dst = reinterpret_cast<uint4*>(base + kOffDesc);
+    for (uint32_t i = t; i < sizeof(NoallocDesc) / 16; i += stride) dst[i] = src[i];
+    if (t < DG_NCOUNTERS) reinterpret_cast<unsigned long long*>(base + kOffCounters)[t] = 0ull;
+    if (t == 0) {
+        *reinterpret_cast<uint32_t*>(base + kOffErr) = 0u;
+        reinterpret_cast<uint32_t*>(base + kOffWhite)[0] = 0xFFFFFFFFu;
+        reinterpret_cast<uint32_t*>(base + kOffWhite)[1] = 0xFFFFFFFFu;
+    }
+    uint32_t* vmark = reinterpret_cast<uint32_t*>(base + kOffVmark);
+    for (uint32_t i = t; i < DG_NOALLOC_MAX_VERTICES / 4; i += stride) vmark[i] = 0u;
+    unsigned long long* vis = reinterpret_cast<unsigned long long*>(base + kOffVis);
+    for (uint32_t i = t; i < npx; i += stride) vis[i] = DG_VIS_EMPTY;
 }
 
 #define NA_CUDA(x)                              \
@@ -226,14 +251,9 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     NA_CUDA(cudaGetDevice(&dev));
     NA_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
 
-    // Pageable source: the copy has taken the descriptor when cudaMemcpyAsync returns.
-    NA_CUDA(cudaMemcpyAsync(base + kOffDesc, &d, sizeof(d), cudaMemcpyHostToDevice, s));
-    // Reset what the previous call left behind.
-    NA_CUDA(cudaMemsetAsync(base + kOffCounters, 0, DG_NCOUNTERS * sizeof(unsigned long long), s));
-    NA_CUDA(cudaMemsetAsync(base + kOffErr, 0, sizeof(uint32_t), s));
-    NA_CUDA(cudaMemsetAsync(base + kOffVmark, 0, (size_t)DG_NOALLOC_MAX_VERTICES * sizeof(uint8_t), s));
-    NA_CUDA(cudaMemsetAsync(base + kOffWhite, 0xFF, 8, s));
-    NA_CUDA(dg_launch_vis_reset(reinterpret_cast<uint64_t*>(base + kOffVis), npx, s));
+    // The descriptor goes by value as a kernel parameter (no host staging buffer).
+    k_noalloc_begin<<<(unsigned)nsm * 4u, 256, 0, s>>>(d, base, (uint32_t)npx);
+    NA_CUDA(cudaGetLastError());
 
     DgLaunchCfg cfg{};
     cfg.cull_blocks = (unsigned)nsm * DG_CULL_BLOCKS_PER_SM;

@@ -281,10 +281,11 @@ __global__ void __launch_bounds__(256) k_tsetup(const DgJobDev job) {
                     bbox_axis(tr.ax, tr.bx, tr.cx, fr.width, tr.xlo, tr.xhi);
                     bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
                     make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
+                    float4* wout = (fr.flags & DG_FRAME_PERSPECTIVE) && job.ttrec_w ? job.ttrec_w + ri : nullptr;
                     if (!clipped)
-                        write_record(job, job.ttrec + ri, sg, tp, tuv, tnr, e, r);
+                        write_record(job, job.ttrec + ri, sg, tp, tuv, tnr, e, r, fr, wout);
                     else
-                        write_clip_record(job, job.ttrec + ri, sg, tp, tuv, tnr, e, tr, P, o, rowbase);
+                        write_clip_record(job, job.ttrec + ri, sg, tp, tuv, tnr, e, tr, P, o, rowbase, fr, wout);
                     px = (tr.xhi - tr.xlo + 1u) * (tr.yhi - tr.ylo + 1u);  // below 2^31: the canvas is smaller
                     job.tbox[ri] = make_uint4(tr.xlo, tr.ylo, tr.xhi - tr.xlo + 1u, sg.frame);
                     job.tmeta[ri] = make_uint2(sg.obj_rank, tseq | (uint32_t)o);
@@ -420,7 +421,8 @@ __global__ void __launch_bounds__(256) k_tfold(const DgJobDev job) {
             const uint32_t rec = __ldcg(job.fval[0] + m);
             float d;
             int errc;
-            uint32_t c = shade_from_record(job, fr, job.ttrec + rec, x, y, inv255, stex, d, errc);
+            const float4* wp = (fr.flags & DG_FRAME_PERSPECTIVE) && job.ttrec_w ? job.ttrec_w + rec : nullptr;
+            uint32_t c = shade_from_record(job, fr, job.ttrec + rec, x, y, inv255, stex, d, errc, wp);
             if (errc != DG_OK) bits |= 1u << errc;
             const float a = __ldcg(job.talpha + rec);
             if (a < 1.0f) c = px_add(px_mul(bg, fS(1.0f, a)), px_mul(c, a));

@@ -42,6 +42,8 @@ SIGNATURES = {
     "dg_ctx_set_tuning": (_i32, [_P, _P]),
     "dg_ctx_get_tuning": (_i32, [_P, _P]),
     "dg_texmap_create": (_i32, [_P, _P, _u64, _u64, _u64, _u64, _P]),
+    "dg_texmap_set_filter": (_i32, [_P, _i32, _i32]),
+    "dg_scene_set_interpolation": (_i32, [_P, _i32, _i32]),
     "dg_object_create": (_i32, [_P, _P, _u64, _P, _u64, _P, _u64, _P, _u64, _P, _u64, _P]),
     "dg_object_destroy": (_i32, [_P, _i32]),
     "dg_scene_create": (_i32, [_P, _u64, _u64, _P]),
@@ -159,6 +161,11 @@ def load_library() -> ctypes.CDLL:
     _lib = lib
     return lib
 
+
+# Extension modes (dg_scene_set_interpolation, dg_texmap_set_filter); the
+# defaults are the reference's behaviour.
+INTERP_AFFINE, INTERP_PERSPECTIVE = 0, 1
+FILTER_NEAREST, FILTER_BILINEAR = 0, 1
 
 # Kernels of one render job in launch order (dg_ctx_kernel_times).
 KERNELS = ["vertex", "cull", "setup_raster", "queue_raster", "resolve"]
@@ -320,6 +327,11 @@ class TextureMap:
                                            ctypes.byref(out)), "TextureMap::new")
         self.id = out.value
         self.width, self.height, self.components = width, height, components
+
+    def set_filter(self, filt: int):
+        """Extension (no counterpart in the reference): FILTER_NEAREST (the
+        reference's get_rgb_slice) or FILTER_BILINEAR (dg_texmap_set_filter)."""
+        _chk(self.ctx.lib.dg_texmap_set_filter(self.ctx.h, self.id, int(filt)), "TextureMap::set_filter")
 
     @staticmethod
     def load_from_file(path: str, ctx: Context | None = None) -> "TextureMap":
@@ -551,6 +563,12 @@ class Scene:
     def set_exponent(self, e: int):
         _chk(self.ctx.lib.dg_scene_set_exponent(self.ctx.h, self.id, int(e)), "set_exponent")
 
+    def set_interpolation(self, mode: int):
+        """Extension (no counterpart in the reference): INTERP_AFFINE (the
+        reference's screen-space interpolation) or INTERP_PERSPECTIVE
+        (dg_scene_set_interpolation)."""
+        _chk(self.ctx.lib.dg_scene_set_interpolation(self.ctx.h, self.id, int(mode)), "set_interpolation")
+
     def frame_setup(self):
         M = np.zeros(16, np.float32)
         P = np.zeros(24, np.float32)
@@ -658,10 +676,15 @@ def build_scene(desc, ctx: Context | None = None) -> BuiltScene:
     """Uploads a draw_gb300.scenes.SceneDesc: texture maps, objects, scene, camera, canvas."""
     ctx = ctx or default_context()
     texmaps = [TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in desc.textures]
+    for t, m in zip(desc.textures, texmaps):
+        if getattr(t, "filter", 0):
+            m.set_filter(t.filter)
     scene = Scene(desc.width, desc.height, ctx)
     scene.camera.reset(desc.cam_pos, desc.cam_dir, float(desc.ratio), desc.near, desc.far, desc.fov_x)
     scene.set_lights(desc.lights)
     scene.set_exponent(desc.exponent)
+    if getattr(desc, "interpolation", 0):
+        scene.set_interpolation(desc.interpolation)
     objects = []
     for o in desc.objects:
         mats = [Texture(f"m{i}", m.ka, m.kd, m.ks, m.alpha, texmaps[m.map_ka] if m.map_ka >= 0 else None,

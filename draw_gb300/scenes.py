@@ -56,6 +56,7 @@ class TextureDesc:
     width: int
     height: int
     comps: int
+    filter: int = 0  # extension: 0 = nearest texel (the reference), 1 = bilinear
 
 
 @dataclass
@@ -72,6 +73,7 @@ class SceneDesc:
     clear_depth: float = float("inf")
     offset: tuple = (0, 0)
     canvas_wh: tuple | None = None  # canvas size when it differs from the scene's (app/mod.rs:58-69)
+    interpolation: int = 0  # extension: 0 = screen-space (the reference), 1 = perspective-correct
     textures: list = field(default_factory=list)
     objects: list = field(default_factory=list)
     name: str = ""

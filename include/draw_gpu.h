@@ -41,6 +41,14 @@ typedef int32_t dg_status;
 
 #define DG_MAX_LIGHTS 8
 
+/* Extensions without a counterpart in the reference (the defaults are the
+ * reference's behaviour): how a scene interpolates its shading attributes and
+ * how a texture map is sampled. */
+#define DG_INTERP_AFFINE 0       /* screen-space barycentrics (canvas.rs:682-722) */
+#define DG_INTERP_PERSPECTIVE 1  /* perspective-correct: weighted by 1/w */
+#define DG_FILTER_NEAREST 0      /* nearest texel (scene/mod.rs:154-168) */
+#define DG_FILTER_BILINEAR 1     /* bilinear blend of four texels */
+
 typedef struct dg_ctx dg_ctx;
 
 /* Material: the reference's `Texture` (scene/mod.rs:206-216). map_ka/map_kd are
@@ -126,6 +134,15 @@ dg_status dg_check_division(dg_ctx* ctx, int32_t mode, uint64_t samples, uint64_
 /* TextureMap::new(img, width, height, components), scene/mod.rs:113-126. */
 dg_status dg_texmap_create(dg_ctx* ctx, const uint8_t* img, uint64_t len, uint64_t width, uint64_t height,
                            uint64_t components, int32_t* out_id);
+/* Extension, no counterpart in the reference (TextureMap::get_rgb_slice,
+ * scene/mod.rs:154-168, samples the nearest texel): DG_FILTER_BILINEAR blends
+ * four texels. x = u*(W-1), y = v*(H-1); the base texel (floor x, floor y) has
+ * the nearest texel's offset; the others are the next column (the same one at
+ * the last column) and the next row up (the same one at the top row). With
+ * c = byte/255, ax = x - floor x, ay = y - floor y, per channel:
+ * t0 = c00*(1-ax) + c01*ax, t1 = c10*(1-ax) + c11*ax, c = t0*(1-ay) + t1*ay.
+ * An offset past the image is DG_E_TEXTURE_RANGE. Default DG_FILTER_NEAREST. */
+dg_status dg_texmap_set_filter(dg_ctx* ctx, int32_t texmap, int32_t filter);
 
 /* ------------------------------------------------------------------- object */
 /* Object::new(name, vertices, normals, texture_vertices, meshes, textures),
@@ -185,6 +202,17 @@ dg_status dg_scene_get_camera(dg_ctx* ctx, int32_t scene, float pos[3], float di
 /* Extensions (reference: one light at Scene.light_source, exponent 2 at canvas.rs:724). */
 dg_status dg_scene_set_lights(dg_ctx* ctx, int32_t scene, const float* pos, uint32_t n);
 dg_status dg_scene_set_exponent(dg_ctx* ctx, int32_t scene, int32_t exponent);
+/* Extension, no counterpart in the reference: DG_INTERP_PERSPECTIVE interpolates
+ * texture coordinates, normals and the light/halfway vectors with
+ * perspective-correct weights. From the reference's screen-space barycentrics
+ * alpha, beta, gama (canvas.rs:673-681) and the vertices' clip-space w (the
+ * projection's divisor, scene/mod.rs:1047-1050): pa = alpha * (1/w_a),
+ * pb = beta * (1/w_b), pc = gama * (1/w_c), s = (pa + pb) + pc, weights
+ * pa/s, pb/s, pc/s, each attribute (a*wa + b*wb) + c*wc in f32 without
+ * contraction. Coverage and depth (the interpolated eye distance) keep the
+ * reference's weights, so they are identical in both modes. Default
+ * DG_INTERP_AFFINE (the reference). */
+dg_status dg_scene_set_interpolation(dg_ctx* ctx, int32_t scene, int32_t mode);
 /* Host frame setup of Scene::render (gen_transformation_matrix, scene/mod.rs:817-899,
  * and Camera::gen_view_planes, :481-593): M row-major, planes near, far, right,
  * left, top, bottom as (normal xyz, k). Updates the camera basis like render. */
@@ -336,12 +364,17 @@ dg_status dg_server_destroy(dg_server* s);
  *
  * The work runs on the calling thread's current device, on `stream` (NULL = the
  * default stream). The first call on a device looks up the scratch array's
- * device address (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the one scratch array, which keeps the last call's
- * contents (each call re-initializes what must start empty): calls whose GPU
- * work overlaps, on different streams or host threads, race and must not be
- * issued. If status_out is not NULL the call waits for its work and stores the
- * device-side status there (DG_OK or DG_E_TEXTURE_RANGE). */
+ * device address (cudaGetSymbolAddress) and keeps it for the life of the
+ * process; make that first call before any stream capture, and do not call the
+ * entry point across a cudaDeviceReset of that device (the kept address would
+ * be stale). The call's job descriptor travels as a kernel parameter, so no
+ * host buffer has to outlive the call. All calls share the one scratch array,
+ * which keeps the last call's contents (each call re-initializes what must
+ * start empty): calls whose GPU work overlaps, on different streams or host
+ * threads, race and must not be issued. If status_out is not NULL the call
+ * waits for its work and stores the first device-side error there: DG_OK,
+ * DG_E_TEXTURE_RANGE (a texel offset past its map), or DG_E_CUDA (an internal
+ * inconsistency, such as a material index beyond the materials passed). */
 #define DG_NOALLOC_MAX_VERTICES 32768u
 #define DG_NOALLOC_MAX_TRIANGLES 65536u
 #define DG_NOALLOC_MAX_PIXELS 262144u

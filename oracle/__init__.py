@@ -64,6 +64,8 @@ def load() -> ctypes.CDLL:
         "or_scene_set_camera": (i32, [P, i32, P, P, f32, f32, f32, f32]),
         "or_scene_set_lights": (i32, [P, i32, P, u32]),
         "or_scene_set_exponent": (i32, [P, i32, i32]),
+        "or_scene_set_interpolation": (i32, [P, i32, i32]),
+        "or_texmap_set_filter": (i32, [P, i32, i32]),
         "or_scene_camera_op": (i32, [P, i32, i32, P]),
         "or_scene_get_camera": (i32, [P, i32, P, P]),
         "or_scene_frame_setup": (i32, [P, i32, P, P]),
@@ -176,6 +178,14 @@ class Oracle:
 
     def set_exponent(self, scene, e: int):
         _chk(self.lib.or_scene_set_exponent(self.ctx, scene, e), "exponent")
+
+    def set_interpolation(self, scene, mode: int):
+        """Extension: 0 = the reference's screen-space interpolation, 1 = perspective-correct."""
+        _chk(self.lib.or_scene_set_interpolation(self.ctx, scene, mode), "interpolation")
+
+    def set_filter(self, texmap: int, filt: int):
+        """Extension: 0 = the reference's nearest texel, 1 = bilinear."""
+        _chk(self.lib.or_texmap_set_filter(self.ctx, texmap, filt), "filter")
 
     def camera_op(self, scene, op: int, v):
         a = np.zeros(3, np.float32)

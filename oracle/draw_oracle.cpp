@@ -201,6 +201,7 @@ struct TextureMap {  // scene/mod.rs:102-126
     std::vector<uint8_t> img;
     uint64_t width = 0, height = 0, components = 0;
     float f_width = 0, f_height = 0;
+    int filter = OR_FILTER_NEAREST;  // extension: OR_FILTER_BILINEAR (no counterpart in the reference)
 };
 std::shared_ptr<TextureMap> texmap_default() {  // scene/mod.rs:128-135 (white, 1x1, 3 comps)
     auto t = std::make_shared<TextureMap>();
@@ -224,6 +225,46 @@ bool get_rgb_slice(const TextureMap& t, float u, float v, uint8_t out[3]) {
     out[2] = t.img[off + 2];
     return true;
 }
+// Extension (no counterpart in the reference, which samples the nearest texel
+// above): bilinear fetch. x = u * (W - 1) and y = v * (H - 1) as in
+// get_rgb_slice; the base texel (x0, y0) = (floor x, floor y) is addressed
+// exactly like the nearest texel (same wrapping offset); its neighbours are
+// x0 + 1 (when x0 + 1 < W, else x0 again) and y0 + 1 (the row above in memory,
+// when that row exists, else y0 again). Every texel's three bytes become
+// byte / 255; per channel, with ax = x - x0 and ay = y - y0:
+//   t0 = c(x0, y0) * (1 - ax) + c(x0 + 1, y0) * ax
+//   t1 = c(x0, y0 + 1) * (1 - ax) + c(x0 + 1, y0 + 1) * ax
+//   c  = t0 * (1 - ay) + t1 * ay
+// evaluated left to right in f32 without contraction. Any of the four offsets
+// past the image is the texture-range error, like the reference's slice index.
+bool get_rgb_bilinear(const TextureMap& t, float u, float v, Vec3& out) {
+    const float x = u * (t.f_width - 1.0f), y = v * (t.f_height - 1.0f);
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float ax = x - fx, ay = y - fy;
+    const uint64_t u_idx = as_usize(fx);
+    const uint64_t v_idx = t.height - 1 - as_usize(fy);
+    const uint64_t off00 = (v_idx * t.width + u_idx) * t.components;
+    const uint64_t dx = (u_idx + 1 < t.width) ? t.components : 0;
+    const uint64_t dy = (v_idx >= 1 && v_idx < t.height) ? t.width * t.components : 0;
+    const uint64_t off[4] = {off00, off00 + dx, off00 - dy, off00 - dy + dx};
+    const uint64_t len = t.img.size();
+    for (int k = 0; k < 4; k++)
+        if (len < 3 || off[k] > len - 3) return false;
+    float ch[3];
+    for (int i = 0; i < 3; i++) {
+        const float c00 = (float)t.img[off[0] + i] / 255.0f, c01 = (float)t.img[off[1] + i] / 255.0f;
+        const float c10 = (float)t.img[off[2] + i] / 255.0f, c11 = (float)t.img[off[3] + i] / 255.0f;
+        const float t0 = c00 * (1.0f - ax) + c01 * ax;
+        const float t1 = c10 * (1.0f - ax) + c11 * ax;
+        ch[i] = t0 * (1.0f - ay) + t1 * ay;
+    }
+    out = V3(ch[0], ch[1], ch[2]);
+    return true;
+}
+// The diffuse/ambient sample of a map under its filter mode (nearest: the
+// reference's get_rgb_slice and Pixel::normalized_as_vec3).
+bool sample_rgb(const TextureMap& t, float u, float v, Vec3& out);
+
 // get_rgba_slice, scene/mod.rs:137-152.
 bool get_rgba_slice(const TextureMap& t, float u, float v, uint8_t out[4]) {
     uint64_t u_idx = as_usize(std::floor(u * t.f_width));
@@ -243,6 +284,14 @@ struct Texture {  // scene/mod.rs:206-216
 Texture texture_default() {  // scene/mod.rs:237-252
     return Texture{V3(0.9f, 0.9f, 0.9f), V3(0.4f, 0.4f, 0.4f), V3(0.5f, 0.5f, 0.5f), 1.0f, texmap_default(),
                    texmap_default()};
+}
+
+bool sample_rgb(const TextureMap& t, float u, float v, Vec3& out) {
+    if (t.filter == OR_FILTER_BILINEAR) return get_rgb_bilinear(t, u, v, out);
+    uint8_t s[3];
+    if (!get_rgb_slice(t, u, v, s)) return false;
+    out = normalized_as_vec3(pixel_new(s[0], s[1], s[2]));
+    return true;
 }
 
 // -------------------------------------------------------------- Canvas state
@@ -314,8 +363,17 @@ inline float powi(float a, int b) {  // LLVM powi lowering: binary exponentiatio
 }
 
 // Canvas::draw_triangle_with_attributes, canvas.rs:577-750 (clipping_rect = None).
+// w holds the three vertices' clip-space w (the projection's fourth row); it is
+// used only by the perspective-correct extension (interp ==
+// OR_INTERP_PERSPECTIVE, no counterpart in the reference): with the reference's
+// screen-space barycentrics alpha, beta, gama,
+//   pa = alpha * (1 / w_a), pb = beta * (1 / w_b), pc = gama * (1 / w_c)
+//   s = (pa + pb) + pc,  qa = pa / s, qb = pb / s, qc = pc / s
+// and texture coordinates, normals, light and halfway vectors are interpolated
+// as (a * qa + b * qb) + c * qc. Coverage and depth (the interpolated eye
+// distance) keep the reference's screen-space barycentrics in both modes.
 void draw_triangle_with_attributes(Canvas& cv, const Attr& A, const Attr& B, const Attr& C, const Texture& tex,
-                                   int nl, int exponent) {
+                                   int nl, int exponent, const float w[3], int interp) {
     Vec2 a = cv.pos_map_center(A.screen_coord - cv.offset);
     Vec2 b = cv.pos_map_center(B.screen_coord - cv.offset);
     Vec2 c = cv.pos_map_center(C.screen_coord - cv.offset);
@@ -353,15 +411,20 @@ void draw_triangle_with_attributes(Canvas& cv, const Attr& A, const Attr& B, con
                   (gama > 0.0f || f_gama * f_gama_out > 0.0f)))
                 continue;
             float pixel_depth = (alpha * a_depth) + (beta * b_depth) + (gama * c_depth);
+            if (interp == OR_INTERP_PERSPECTIVE) {
+                const float pa = alpha * (1.0f / w[0]), pb = beta * (1.0f / w[1]), pc = gama * (1.0f / w[2]);
+                const float sw = (pa + pb) + pc;
+                alpha = pa / sw;
+                beta = pb / sw;
+                gama = pc / sw;
+            }
             Vec3 ptc = (A.texture_coord * alpha) + (B.texture_coord * beta) + (C.texture_coord * gama);
-            uint8_t dsl[3], asl[3];
-            if (!get_rgb_slice(*tex.map_kd, ptc.x(), ptc.y(), dsl) ||
-                !get_rgb_slice(*tex.map_ka, ptc.x(), ptc.y(), asl)) {
+            Vec3 diffuse, ambient;
+            if (!sample_rgb(*tex.map_kd, ptc.x(), ptc.y(), diffuse) ||
+                !sample_rgb(*tex.map_ka, ptc.x(), ptc.y(), ambient)) {
                 cv.err = OR_E_TEXTURE_RANGE;
                 return;
             }
-            Vec3 diffuse = normalized_as_vec3(pixel_new(dsl[0], dsl[1], dsl[2]));
-            Vec3 ambient = normalized_as_vec3(pixel_new(asl[0], asl[1], asl[2]));
             Vec3 pn = (A.normal * alpha) + (B.normal * beta) + (C.normal * gama);
             Vec3 c_l = tex.ks;
             Vec3 c_r = color_multiply(diffuse, tex.kd);
@@ -601,6 +664,7 @@ struct Scene {  // scene/mod.rs:749-757
     std::vector<int32_t> objects;
     std::vector<Vec3> lights;
     int exponent = 2;
+    int interpolation = OR_INTERP_AFFINE;  // extension: OR_INTERP_PERSPECTIVE
 };
 
 }  // namespace
@@ -712,6 +776,18 @@ int32_t or_scene_set_lights(or_ctx* c, int32_t scene, const float* pos, uint32_t
     auto& s = c->scenes[scene];
     s.lights.clear();
     for (uint32_t i = 0; i < n; i++) s.lights.push_back(V3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+    return OR_OK;
+}
+
+int32_t or_scene_set_interpolation(or_ctx* c, int32_t scene, int32_t mode) {
+    if (scene < 0 || (size_t)scene >= c->scenes.size() || mode < 0 || mode > 1) return -OR_E_INVALID;
+    c->scenes[scene].interpolation = mode;
+    return OR_OK;
+}
+
+int32_t or_texmap_set_filter(or_ctx* c, int32_t texmap, int32_t filter) {
+    if (texmap < 0 || (size_t)texmap >= c->texmaps.size() || filter < 0 || filter > 1) return -OR_E_INVALID;
+    c->texmaps[texmap]->filter = filter;
     return OR_OK;
 }
 
@@ -901,13 +977,16 @@ static void assemble(const Object& o, const uint32_t* q, const std::vector<Attr>
 }
 
 // Projection of one clipped triangle and its draw call, scene/mod.rs:1047-1083.
-static void project_and_draw(Canvas& cv, const Matrix4& M, Triangle& ct, const Texture& tex, int nl, int exponent) {
+static void project_and_draw(Canvas& cv, const Matrix4& M, Triangle& ct, const Texture& tex, int nl, int exponent,
+                             int interp) {
+    float ws[3];
     for (int k = 0; k < 3; k++) {
         Vec4 p = M * as_vec4(ct.v[k]);
         float w = p.a[3];
+        ws[k] = w;
         ct.at[k].screen_coord = Vec2{p.a[0], p.a[1]} / w;
     }
-    draw_triangle_with_attributes(cv, ct.at[0], ct.at[1], ct.at[2], tex, nl, exponent);
+    draw_triangle_with_attributes(cv, ct.at[0], ct.at[1], ct.at[2], tex, nl, exponent, ws, interp);
 }
 
 // Scene::render, scene/mod.rs:901-1249.
@@ -956,7 +1035,7 @@ int32_t or_scene_render(or_ctx* c, int32_t scene, int32_t canvas) {
                 if (tri_eye.dot(n) <= 0.0f) continue;  // back-face culling, :1016-1027
                 int cnt = clip_against_planes(t, planes, clipped, nl);
                 for (int k = 0; k < cnt; k++) {
-                    project_and_draw(cv, M, clipped[k], tex, nl, s.exponent);
+                    project_and_draw(cv, M, clipped[k], tex, nl, s.exponent, s.interpolation);
                     if (cv.err) return -cv.err;
                 }
             }
@@ -989,7 +1068,7 @@ int32_t or_scene_render(or_ctx* c, int32_t scene, int32_t canvas) {
                 assemble(o, &m.tris[9 * ti], vis, t, nl);
                 int cnt = clip_against_planes(t, planes, clipped, nl);
                 for (int k = 0; k < cnt; k++) {
-                    project_and_draw(cv, M, clipped[k], tex, nl, s.exponent);
+                    project_and_draw(cv, M, clipped[k], tex, nl, s.exponent, s.interpolation);
                     if (cv.err) return -cv.err;
                 }
             }

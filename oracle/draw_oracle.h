@@ -85,6 +85,17 @@ int32_t or_scene_set_camera(or_ctx* c, int32_t scene, const float pos[3], const 
                             float near_, float far_, float fov_x_deg);
 int32_t or_scene_set_lights(or_ctx* c, int32_t scene, const float* pos, uint32_t n);
 int32_t or_scene_set_exponent(or_ctx* c, int32_t scene, int32_t exponent);
+/* Extensions without a counterpart in the reference (defaults = the reference):
+ * interpolation of the shading attributes (OR_INTERP_AFFINE: the reference's
+ * screen-space barycentrics; OR_INTERP_PERSPECTIVE: weighted by 1/w, see
+ * draw_triangle_with_attributes) and a texture map's filter (OR_FILTER_NEAREST:
+ * get_rgb_slice; OR_FILTER_BILINEAR: get_rgb_bilinear). */
+#define OR_INTERP_AFFINE 0
+#define OR_INTERP_PERSPECTIVE 1
+#define OR_FILTER_NEAREST 0
+#define OR_FILTER_BILINEAR 1
+int32_t or_scene_set_interpolation(or_ctx* c, int32_t scene, int32_t mode);
+int32_t or_texmap_set_filter(or_ctx* c, int32_t texmap, int32_t filter);
 /* Camera movement, scene/mod.rs:377-413, 430-432, 803-813. op: 0 up,1 down,2 left,3 right,4 foward,5 backward,
  * 6 rotate_origin(deg), 7 set_pos(v3), 8 move_camera_direction(dx,dy as ints in v[0],v[1]). */
 int32_t or_scene_camera_op(or_ctx* c, int32_t scene, int32_t op, const float* v);

@@ -17,10 +17,15 @@ def oracle_render(desc, o=None, frames: int = 1, camera_ops=()):
 
     o = o or _oracle.Oracle()
     texs = [o.texmap(t.img, t.width, t.height, t.comps) for t in desc.textures]
+    for t, i in zip(desc.textures, texs):
+        if getattr(t, "filter", 0):
+            o.set_filter(i, t.filter)
     s = o.scene(desc.width, desc.height)
     o.set_camera(s, desc.cam_pos, desc.cam_dir, desc.ratio, desc.near, desc.far, desc.fov_x)
     o.set_lights(s, desc.lights)
     o.set_exponent(s, desc.exponent)
+    if getattr(desc, "interpolation", 0):
+        o.set_interpolation(s, desc.interpolation)
     for ob in desc.objects:
         mats = [dict(ka=m.ka, kd=m.kd, ks=m.ks, alpha=m.alpha, map_ka=texs[m.map_ka] if m.map_ka >= 0 else -1,
                      map_kd=texs[m.map_kd] if m.map_kd >= 0 else -1) for m in ob.materials]
@@ -39,6 +44,17 @@ def oracle_render(desc, o=None, frames: int = 1, camera_ops=()):
             break
     f = o.read(c, cw, ch)
     return f.bgra, f.depth, st
+
+
+def oracle_render_many(descs, threads: int | None = None):
+    """oracle_render of every desc, on host threads (one oracle context per
+    call; ctypes releases the GIL while a frame renders)."""
+    import concurrent.futures as cf
+    import os
+
+    n = threads or min(len(descs), os.cpu_count() or 1) or 1
+    with cf.ThreadPoolExecutor(n) as ex:
+        return list(ex.map(oracle_render, descs))
 
 
 def gpu_render(desc, ctx, frames: int = 1, camera_ops=()):

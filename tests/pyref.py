@@ -239,6 +239,37 @@ def texel(img, w, h, comps, u, v):
     return [F(int(img[off + k])) / F(255) for k in range(3)]
 
 
+def texel_bilinear(img, w, h, comps, u, v):
+    """Extension (no counterpart in the reference): the bilinear blend of the
+    base texel (addressed like the nearest one) and its right, upper and
+    upper-right neighbours (clamped at the image's last column and first row),
+    per channel t0 = c00 (1 - ax) + c01 ax, t1 = c10 (1 - ax) + c11 ax,
+    c = t0 (1 - ay) + t1 ay."""
+    x, y = u * (F(w) - F(1)), v * (F(h) - F(1))
+    fx, fy = np.floor(x), np.floor(y)
+    ax, ay = x - fx, y - fy
+    ui = usize(fx)
+    vi = (h - 1 - usize(fy)) % 2 ** 64
+    o00 = ((vi * w + ui) * comps) % 2 ** 64
+    dx = comps if ui + 1 < w else 0
+    dy = w * comps if 1 <= vi < h else 0
+    offs = [o00, (o00 + dx) % 2 ** 64, (o00 - dy) % 2 ** 64, (o00 - dy + dx) % 2 ** 64]
+    for o in offs:
+        if o + 3 > len(img):
+            raise IndexError("texel offset out of range")
+    out = []
+    for k in range(3):
+        c00, c01, c10, c11 = (F(int(img[o + k])) / F(255) for o in offs)
+        t0 = c00 * (F(1) - ax) + c01 * ax
+        t1 = c10 * (F(1) - ax) + c11 * ax
+        out.append(t0 * (F(1) - ay) + t1 * ay)
+    return out
+
+
+def sample(img, w, h, comps, filt, u, v):
+    return texel_bilinear(img, w, h, comps, u, v) if filt else texel(img, w, h, comps, u, v)
+
+
 def powi(x, e):
     r = F(1)
     n = e
@@ -280,10 +311,10 @@ def render(desc):
                 maps = []
                 for mi in (mat.map_kd, mat.map_ka):
                     if mi < 0:
-                        maps.append((np.array([255, 255, 255], np.uint8), 1, 1, 3))
+                        maps.append((np.array([255, 255, 255], np.uint8), 1, 1, 3, 0))
                     else:
                         t = desc.textures[mi]
-                        maps.append((t.img, t.width, t.height, t.comps))
+                        maps.append((t.img, t.width, t.height, t.comps, getattr(t, "filter", 0)))
                 for row in mesh.tris:
                     vi, ti, ni = row[0:3], row[3:6], row[6:9]
                     a, b, c = V[vi[0]], V[vi[1]], V[vi[2]]
@@ -301,16 +332,18 @@ def render(desc):
                             attr[f"h{li}"] = vis["half"][li]
                         verts.append((V[vi[k]], attr))
                     for tri in clip(pls, tuple(verts)):
-                        centres = []
+                        centres, ws = [], []
                         for p, _ in tri:
                             hh = m_vec(M, [p[0], p[1], p[2], F(1)])
                             sx, sy = hh[0] / hh[3], hh[1] / hh[3]
+                            ws.append(hh[3])
                             centres.append((np.floor((sx + (-off[0])) + F(0.5)), np.floor((sy + (-off[1])) + F(0.5))))
-                        _raster(tri, centres, mat, maps, len(lights), desc.exponent, W, H, frame, depth)
+                        _raster(tri, centres, mat, maps, len(lights), desc.exponent, W, H, frame, depth, ws,
+                                getattr(desc, "interpolation", 0))
     return frame, depth
 
 
-def _raster(tri, cs, mat, maps, nl, exponent, W, H, frame, depth):
+def _raster(tri, cs, mat, maps, nl, exponent, W, H, frame, depth, ws, interp):
     A, B, C = cs
     x0, x1 = axis_range([A[0], B[0], C[0]], W)
     y0, y1 = axis_range([A[1], B[1], C[1]], H)
@@ -331,27 +364,31 @@ def _raster(tri, cs, mat, maps, nl, exponent, W, H, frame, depth):
             if not ((al > 0 or ta) and (be > 0 or tb) and (ga > 0 or tg)):
                 continue
 
-            def mix(key):
+            def mix(key, wa, wb, wc):
                 u, v, w = at[0][key], at[1][key], at[2][key]
                 if isinstance(u, tuple):
-                    return tuple((p * al + q * be) + r * ga for p, q, r in zip(u, v, w))
-                return (al * u + be * v) + ga * w
+                    return tuple((p * wa + q * wb) + r * wc for p, q, r in zip(u, v, w))
+                return (wa * u + wb * v) + wc * w
 
-            d = mix("depth")
-            uv = mix("uv")
-            dif = texel(*maps[0], uv[0], uv[1])
-            amb = texel(*maps[1], uv[0], uv[1])
-            nrm = mix("normal")
+            d = mix("depth", al, be, ga)
+            if interp:  # extension: attributes weighted by 1/w, depth and coverage as the reference
+                pa, pb, pc = al * (F(1) / ws[0]), be * (F(1) / ws[1]), ga * (F(1) / ws[2])
+                s = (pa + pb) + pc
+                al, be, ga = pa / s, pb / s, pc / s
+            uv = mix("uv", al, be, ga)
+            dif = sample(*maps[0], uv[0], uv[1])
+            amb = sample(*maps[1], uv[0], uv[1])
+            nrm = mix("normal", al, be, ga)
             c_r = tuple(dif[i] * kd[i] for i in range(3))
             c_a = tuple(amb[i] * ka[i] for i in range(3))
             inner = c_a
             for li in range(nl):
-                ln = v_dot(mix(f"l{li}"), nrm)
+                ln = v_dot(mix(f"l{li}", al, be, ga), nrm)
                 mx = ln if ln > 0 else F(0)
                 inner = v_add(inner, v_scale(ks, F(1) - mx))
             col = tuple(c_r[i] * inner[i] for i in range(3))
             for li in range(nl):
-                col = v_add(col, v_scale(ks, powi(v_dot(mix(f"h{li}"), nrm), exponent)))
+                col = v_add(col, v_scale(ks, powi(v_dot(mix(f"h{li}", al, be, ga), nrm), exponent)))
             sc = v_scale(col, F(255))
             if d < depth[y, x]:
                 frame[H - 1 - y, x] = (u8(sc[2]), u8(sc[1]), u8(sc[0]), 255)

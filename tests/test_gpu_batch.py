@@ -79,6 +79,43 @@ def test_graph_batch_matches_plain_path(gpu_ctx):
         batch.close()
 
 
+def test_batch_config_full_size_equals_oracle(gpu_ctx, oracle_lib):
+    """The batching configuration at its stated size, the exact batch bench.py
+    times: 256 frames of side 128..512 (log-uniform), meshes of 1k..200k
+    triangles, textures 256^2..1024^2 from a pool of 32. Every frame of the
+    one-launch-per-stage batch (dg_render_batch) and of its graph replay
+    (dg_batch_render) equals the oracle's render of it."""
+    from draw_gb300 import renderer
+    from helpers import oracle_render_many
+
+    frames = S.batch_frames(n_frames=256, seed=1234)
+    assert len(frames) == 256
+    refs = oracle_render_many(frames)
+    built = [renderer.build_scene(d, gpu_ctx) for d in frames]
+    sc, cv = [b.scene for b in built], [b.canvas for b in built]
+
+    def check(tag):
+        bad = []
+        for d, b, ref in zip(frames, built, refs):
+            got = (*b.canvas.read(), 0)
+            p = compare(ref, got, d.clear_depth)
+            if not p.ok:
+                bad.append(f"{tag} {d.name}: {describe(p)}; {first_mismatch(ref, got)}")
+        assert not bad, "\n".join(bad[:5]) + f"\n({len(bad)} frames differ)"
+
+    gpu_ctx.render_batch(sc, cv)
+    check("render_batch")
+    for b in built:
+        b.canvas.clear()
+    batch = gpu_ctx.batch(sc, cv)
+    try:
+        batch.render()
+        batch.render()
+        check("graph replay")
+    finally:
+        batch.close()
+
+
 def test_autotune_sets_valid_tuning_and_keeps_results(gpu_ctx, oracle_lib, tmp_path):
     from draw_gb300 import autotune, renderer
 

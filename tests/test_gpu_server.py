@@ -90,6 +90,65 @@ def test_server_mix_equals_alone(gpu_ctx):
     ctx.close()
 
 
+def test_server_large_frames_in_the_mix(gpu_ctx, oracle_lib):
+    """The serving configuration's large requests: 1920x1080 and 3840x2160 frames
+    of a 1M-triangle sphere and a 2M-triangle torus, submitted together with
+    256^2 and 512^2 frames of small meshes. Each result equals the same request
+    rendered alone, and the large frames equal the oracle's render."""
+    from draw_gb300 import renderer as R
+    from helpers import oracle_render_many
+
+    meshes = [S.mesh_for_tris("sphere", 1_000_000), S.mesh_for_tris("torus", 2_000_000),
+              S.mesh_for_tris("torus", 5_000), S.mesh_for_tris("sphere", 20_000)]
+    assert meshes[0][3].shape[0] >= 1_000_000 and meshes[1][3].shape[0] >= 1_900_000
+    texs = [S.value_noise_checker(512, 512, 11), S.value_noise_checker(1024, 1024, 12)]
+    objs = []
+    for i, (pos, nrm, uv, tri) in enumerate(meshes):
+        mat = S.Material((0.1,) * 3, (0.7,) * 3, (0.2,) * 3, 1.0, i % 2, i % 2)
+        objs.append(S.ObjectDesc(pos, nrm, uv, [S.MeshDesc(S._tris9(tri), 0)], [mat]))
+    rng = np.random.Generator(np.random.PCG64(77))
+    sizes = [(1920, 1080, 0), (3840, 2160, 0), (3840, 2160, 1), (1920, 1080, 1)]
+    reqs = []
+    for k in range(16):
+        if k % 4 == 1:
+            w, h, oi = sizes[k // 4]
+        else:
+            w, h = [(256, 256), (512, 512)][k % 2]
+            oi = 2 + (k % 3 == 0)
+        az, el, dist = rng.uniform(0, 2 * math.pi), rng.uniform(0.1, 1.0), rng.uniform(2.6, 4.0)
+        cam = (dist * math.cos(el) * math.sin(az), dist * math.sin(el), dist * math.cos(el) * math.cos(az))
+        light = [(3.0 * math.sin(az + 1), 4.0, 3.0 * math.cos(az + 1))]
+        reqs.append((oi, w, h, cam, light, 2, float("inf")))
+    ref = _alone(objs, texs, reqs)
+    large = [k for k, r in enumerate(reqs) if r[1] >= 1920]
+    descs = []
+    for k in large:
+        oi, w, h, cam, light, e, clear = reqs[k]
+        descs.append(S.SceneDesc(w, h, cam_pos=cam, cam_dir=tuple(-c for c in cam), near=-0.5, far=-100.0,
+                                 fov_x=60.0, lights=np.array(light, np.float32), exponent=e, clear_depth=clear,
+                                 textures=texs, objects=[objs[oi]]))
+    oref = dict(zip(large, oracle_render_many(descs)))
+    ctx = R.Context(0)
+    tm = [R.TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in texs]
+    obs = [R.upload_object(o, tm, ctx) for o in objs]
+    srv = R.Server(ctx, budget_bytes=8 << 30, max_batch=16, streams=3)
+    tickets = []
+    for oi, w, h, cam, light, e, clear in reqs:
+        tickets.append(srv.submit(R.Server.request(obs[oi], w, h, cam, tuple(-c for c in cam), -0.5, -100.0, 60.0,
+                                                   light, e, clear)))
+    for k, (oi, w, h, *_r) in enumerate(reqs):
+        bgra, depth, _lat = srv.wait(tickets[k], w, h, read=True)
+        p = compare(ref[k], (bgra, depth), reqs[k][6])
+        assert p.ok, f"request {k} ({w}x{h}) vs alone: {describe(p)}"
+        if k in oref:
+            q = compare(oref[k], (bgra, depth), reqs[k][6])
+            assert q.ok and q.n_covered > 0, f"request {k} ({w}x{h}) vs oracle: {describe(q)}"
+    st = srv.stats()
+    assert st["completed"] == len(reqs) and st["error"] == 0
+    srv.close()
+    ctx.close()
+
+
 def test_server_admission_respects_budget(gpu_ctx):
     from draw_gb300 import renderer as R
 

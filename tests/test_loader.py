@@ -5,9 +5,10 @@ The parser is checked bit for bit against an independent restatement in
 numpy float32 below (the same rules: quad split (a,b,c),(c,d,a); normals
 normalized; positions scaled to max |v| = 100; per-group dummy texture
 coordinate and generated smooth normals; materials after Texture::default()).
-The reference's own model files are parsed when the reference tree is
-present (triangle counts; fgc_skeleton's material lacks Ka, on which the
-reference panics)."""
+The reference's own model files are parsed too (triangle counts): the donut,
+lemur and soldier1 models are vendored under tests/fixtures/models as test
+data; fgc_skeleton (whose material lacks Ka, on which the reference panics) is
+parsed when DRAW_REF_MODELS names a directory holding the reference's models."""
 import ctypes
 import os
 import struct
@@ -20,7 +21,17 @@ from draw_gb300 import imageio
 from draw_gb300 import renderer as R
 
 F = np.float32
-REF_MODELS = "/root/reference/models"
+FIXTURE_MODELS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "fixtures", "models")
+REF_MODELS = os.environ.get("DRAW_REF_MODELS", "")
+
+
+def model_path(model: str) -> str | None:
+    """A model file from the vendored fixtures, else from DRAW_REF_MODELS."""
+    for root in (FIXTURE_MODELS, REF_MODELS):
+        if root and os.path.exists(os.path.join(root, model)):
+            return os.path.join(root, model)
+    return None
+
 
 OBJ_TEXT = """# quads, triangles, groups, materials, negative indices
 mtllib m.mtl
@@ -245,12 +256,14 @@ def test_load_from_file_python_mirror(lib, tmp_path):
     assert (w, hh, comps) == (6, 4, 4)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_MODELS), reason="reference model files not present")
 @pytest.mark.parametrize("model,ntri,status", [("donut/donut.obj", 2048, 0), ("lemur/lemur.obj", 1972, 0),
                                                ("soldier1/soldier1.obj", 3144, 0),
                                                ("skeleton/fgc_skeleton.obj", 0, 1)])
 def test_reference_models(lib, model, ntri, status):
-    st, h = _parse(lib, os.path.join(REF_MODELS, model))
+    path = model_path(model)
+    if path is None:
+        pytest.skip(f"{model} is not vendored and DRAW_REF_MODELS is not set")
+    st, h = _parse(lib, path)
     assert st == status
     if st == 0:
         cnt = (ctypes.c_uint64 * 6)()

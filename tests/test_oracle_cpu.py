@@ -142,3 +142,22 @@ def test_pyref_matches_oracle_torus():
     py = pyref.render(d)
     p = compare(ref, (py[0], py[1]), d.clear_depth)
     assert p.ok and p.colour_max_lsb == 0 and p.n_covered > 500, describe(p)
+
+
+@pytest.mark.parametrize("interp,filt", [(1, 0), (0, 1), (1, 1)])
+def test_pyref_matches_oracle_extension_modes(interp, filt):
+    """The opt-in extensions (perspective-correct attribute interpolation,
+    bilinear texture fetch) restated twice agree bit for bit; coverage and
+    depth equal the reference mode's, and the colours differ from it."""
+    d = S.torus_scene(width=72, height=54, nu=20, nv=8, tex=64, exponent=32)
+    d.cam_pos = (0.3, 1.1, 1.7)
+    d.cam_dir = tuple(-c for c in d.cam_pos)
+    base = oracle_render(d)
+    d.interpolation = interp
+    d.textures[0].filter = filt
+    ref = oracle_render(d)
+    py = pyref.render(d)
+    p = compare(ref, (py[0], py[1]), d.clear_depth)
+    assert p.ok and p.colour_max_lsb == 0 and p.n_covered > 500, describe(p)
+    q = compare(base, (ref[0], ref[1]), d.clear_depth)
+    assert q.coverage_equal and q.depth_bits_equal and q.colour_frac_diff > 0.05, describe(q)

@@ -6,10 +6,13 @@ device).
 
 The test calls it through the C ABI, twice in a row on the library's one
 shared scratch array, and checks each frame against what the allocating entry
-point (dg_scene_render through the Scene/Canvas API) renders for the same scene:
-coverage and depth bit-exact, colour within COLOUR_TOL_LSB. The device buffers
-for the inputs and outputs are the caller's (allocated here with torch before
-the call); the entry point itself allocates nothing.
+point (dg_scene_render through the Scene/Canvas API) renders for the same scene
+and against the CPU oracle: coverage and depth bit-exact, colour within
+COLOUR_TOL_LSB. A second test runs a mesh at the triangle limit, with many
+triangles across the near plane, then a small mesh after it (the scratch keeps
+the large call's contents) on a caller's stream without status_out. The device
+buffers for the inputs and outputs are the caller's (allocated here with torch
+before the call); the entry point itself allocates nothing.
 
 Kept in a file of its own that pytest collects last, so a run that stops at the
 first failure has already run every other test."""
@@ -19,7 +22,7 @@ import numpy as np
 import pytest
 
 from draw_gb300 import scenes as S
-from helpers import COLOUR_TOL_LSB, compare, describe
+from helpers import COLOUR_TOL_LSB, compare, describe, oracle_render
 
 pytestmark = pytest.mark.gpu
 
@@ -54,7 +57,7 @@ def _device_texmap(torch, t):
     return dg_device_texmap(d.data_ptr(), n, t.width, t.height, t.comps), d
 
 
-def _render_noalloc(lib, torch, desc, mesh, texmaps):
+def _render_noalloc(lib, torch, desc, mesh, texmaps, stream=None, want_status=True):
     from draw_gb300 import renderer as R
 
     ob = desc.objects[0]
@@ -80,9 +83,13 @@ def _render_noalloc(lib, torch, desc, mesh, texmaps):
     status = ctypes.c_int32(-1)
     st = lib.dg_render_noalloc(ctypes.byref(p), ctypes.byref(mesh), ctypes.cast(mats, ctypes.c_void_p),
                                len(ob.materials), ctypes.cast(tex, ctypes.c_void_p), len(texmaps), bgra.data_ptr(),
-                               depth.data_ptr(), None, ctypes.byref(status))
+                               depth.data_ptr(), None if stream is None else ctypes.c_void_p(stream.cuda_stream),
+                               ctypes.byref(status) if want_status else None)
     assert st == 0, st
-    assert status.value == 0, status.value
+    if want_status:
+        assert status.value == 0, status.value
+    else:
+        stream.synchronize()
     return bgra.cpu().numpy().reshape(ch, cw, 4), depth.cpu().numpy().reshape(ch, cw)
 
 
@@ -112,6 +119,36 @@ def test_noalloc_matches_allocating_path_twice(gpu_ctx):
         ref = _render_allocating(gpu_ctx, desc)
         p = compare(ref, got, desc.clear_depth)
         assert p.ok and p.colour_max_lsb <= COLOUR_TOL_LSB and p.n_covered > 1000, describe(p)
+        q = compare(oracle_render(desc), got, desc.clear_depth)
+        assert q.ok and q.colour_max_lsb <= COLOUR_TOL_LSB, describe(q)
+
+
+def test_noalloc_at_its_limits_then_small_on_a_stream(gpu_ctx, oracle_lib):
+    """A torus of 64,512 triangles (32,637 vertices, within the 65,536 / 32,768
+    limits) on a 512x512 canvas (the pixel limit), seen from above with the near
+    plane slicing its top (about a thousand triangles cross it); then a small mesh rendered after
+    it on a non-default stream with status_out NULL, the caller synchronizing
+    the stream. Both frames equal the allocating path's and the oracle's."""
+    torch = pytest.importorskip("torch")
+    from draw_gb300 import renderer as R
+
+    lib = R.load_library()
+    big = S.torus_scene(width=512, height=512, nu=252, nv=128, tex=64, exponent=2)
+    big.cam_pos = (0.0, 1.2, 0.0)
+    big.cam_dir = (0.05, -1.0, 0.02)
+    big.near, big.far = -1.15, -50.0
+    assert big.n_tris == 64_512 and big.objects[0].vertices.shape[0] <= 32_768
+    small = S.torus_scene(width=160, height=120, nu=12, nv=6, tex=32, exponent=5)
+    stream = torch.cuda.Stream()
+    for desc, kw in ((big, {}), (small, dict(stream=stream, want_status=False))):
+        mesh, keep = _device_mesh(torch, desc.objects[0])
+        texmaps, keep_t = zip(*[_device_texmap(torch, t) for t in desc.textures])
+        got = _render_noalloc(lib, torch, desc, mesh, list(texmaps), **kw)
+        ref = _render_allocating(gpu_ctx, desc)
+        p = compare(ref, got, desc.clear_depth)
+        assert p.ok and p.n_covered > 1000, describe(p)
+        q = compare(oracle_render(desc), got, desc.clear_depth)
+        assert q.ok, describe(q)
 
 
 def test_noalloc_rejects_sizes_beyond_its_limits(gpu_ctx):
