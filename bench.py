@@ -68,6 +68,13 @@ def parse():
     return ap.parse_args()
 
 
+def bench_config(world: int) -> dict:
+    """The `config` object both arms print (the same workload and policy)."""
+    return {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+            "l2": "GPU arm: flushed before every timed step (256 MiB write); CPU arm: no flush",
+            "resident_inputs": True}
+
+
 def headline_scene():
     from draw_gb300 import scenes
 
@@ -266,15 +273,18 @@ class OracleFarm:
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
+    world = 1  # rank 0 alone runs the CPU arm
     desc = headline_scene()
     threads = os.cpu_count() or 1
     farm = OracleFarm(desc, threads)
     t1, _ = farm.single()
-    # Each step renders one frame per host thread; the number of timed steps is
-    # capped so the whole arm stays within about two minutes of CPU time.
-    warm = min(args.warmup, 3)
+    # Each step renders one frame per host thread (all threads in parallel, so a
+    # step takes about one single-thread frame time); the requested warm-up is
+    # honoured and the timed steps are capped so the arm stays within about two
+    # minutes.
+    warm = args.warmup
     step_s = max(t1, 1e-3)
-    steps = max(1, min(args.steps, int(90.0 / step_s)))
+    steps = max(1, min(args.steps, int(120.0 / step_s)))
     for _ in range(warm):
         farm.run(1)
     wall = sum(farm.run(1) for _ in range(steps))
@@ -284,7 +294,7 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * wall / steps, "steps_requested": args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
+        "data": "synthetic (seeded UV-sphere field)", "config": bench_config(world),
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
                          "sample": f"each step renders one frame per host thread ({threads} threads); "
                                    f"single-thread frame time {t1 * 1000:.1f} ms"},
@@ -403,8 +413,7 @@ def run_ours(args, world, rank, local):
         "metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded UV-sphere field)",
-        "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
-                   "l2": "flushed before every timed step (256 MiB write)", "resident_inputs": True},
+        "config": bench_config(world),
         "mtris_per_s": value * desc.n_tris / 1e6,
         "mshaded_frags_per_s": value * stats["covered_pixels"] / 1e6,
         "wall_ms_per_step": 1000.0 * wall / args.steps,
@@ -454,9 +463,39 @@ def run_ours(args, world, rank, local):
                           "coverage_equal": bool(np.array_equal(np.isfinite(first.depth), np.isfinite(depth))),
                           "colour_max_lsb": int(diff.max()), "colour_frac_diff": float((diff.max(-1) > 0).mean())}
     if rank == 0:
+        line["summary"] = summary(line)
         print(json.dumps(line), flush=True)
     ctx.close()
     return 0
+
+
+def summary(line: dict) -> dict:
+    """The numbers the other keys hold in detail, last on the line."""
+    out = {"frames_per_s": round(line["value"], 1), "e2e_frames_per_s": round(line["e2e"]["value"], 1),
+           "frame_roofline_frac": round(line["frame_roofline"]["frac"], 4),
+           "kernel_roofline_frac": round(line["roofline"]["frac"], 4),
+           "kernels_us": {k: round(v * 1000.0, 1) for k, v in line["kernels_ms"].items()}}
+    if "batched" in line:
+        b = line["batched"]
+        out["batched_speedup"] = round(b["speedup"], 2)
+        out["graph_speedup"] = round(b["graph_speedup"], 2)
+        out["batched_frames_per_s"] = round(b["batched_frames_per_s"], 1)
+    if "served" in line:
+        s = line["served"]
+        out["served_saturated_vs_plain"] = round(s["saturated_vs_plain"], 2)
+        out["served_p50_ms"] = round(s["p50_ms"], 3)
+        out["served_p99_ms"] = round(s["p99_ms"], 3)
+        out["served_p99_over_p50"] = round(s["p99_over_p50"], 2) if s["p99_over_p50"] else None
+    if "stress" in line:
+        out["stress_ms"] = round(min(line["stress"]["ms_per_frame_default"], line["stress"]["ms_per_frame_tuned"]), 3)
+    if "torus" in line:
+        out["torus_us"] = round(line["torus"]["ms_per_frame"] * 1000.0, 1)
+    if "cpu_baseline" in line:
+        out["cpu_frames_per_s"] = round(line["cpu_baseline"]["value"], 2)
+    if "parity" in line:
+        p = line["parity"]
+        out["parity"] = f"depth_bits_equal={p['depth_bits_equal']} colour_max_lsb={p['colour_max_lsb']}"
+    return out
 
 
 def batched_leg(ctx, stream, n_frames: int) -> dict:
@@ -700,12 +739,16 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
             cv.init_depth(float("inf"))
             canvases[(w, h)] = cv
 
-    def run_plain():
-        for oi, w, h, cam, light in plain_reqs:
+    def run_plain(evs=None):
+        for k, (oi, w, h, cam, light) in enumerate(plain_reqs):
             sc = scenes[(oi, w, h)]
             sc.camera.reset(cam, tuple(-c for c in cam), float(np.float32(w) / np.float32(h)), -0.5, -100.0, 60.0)
             sc.set_lights(light)
+            if evs is not None:
+                evs[k][0].record(stream)
             sc.render(canvases[(w, h)])
+            if evs is not None:
+                evs[k][1].record(stream)
 
     with torch.cuda.stream(stream):
         run_plain()
@@ -717,7 +760,14 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
         e1.record(stream)
         torch.cuda.synchronize()
         plain_wall = time.perf_counter() - w0
+        # per-request device time of the same loop, by resolution class
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in plain_reqs]
+        run_plain(evs)
+        torch.cuda.synchronize()
     plain_dev = e0.elapsed_time(e1) / 1e3
+    plain_class_ms = {}
+    for (oi, w, h, *_r), (a, b_) in zip(plain_reqs, evs):
+        plain_class_ms.setdefault(f"{w}x{h}", []).append(a.elapsed_time(b_))
     ctx.set_stream(None)
 
     srv = R.Server(ctx, budget_bytes=budget, max_batch=64, streams=3)
@@ -742,16 +792,19 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
     # 3) Poisson arrivals at `rate` for `seconds`
     n = int(rate * seconds)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
-    pois_reqs = [req(q) for q in sample(n)]
+    pois_q = sample(n)
+    pois_reqs = [req(q) for q in pois_q]
+    pois_classes = [f"{q[1]}x{q[2]}" for q in pois_q]
     srv.reset_stats()
     tq = []
     done = th.Event()
+    lat = [0.0] * n
 
     def waiter():
         i = 0
         while i < n:
             if i < len(tq):
-                srv.wait(tq[i])
+                lat[i] = srv.wait(tq[i])[2]
                 i += 1
             else:
                 time.sleep(0.0002)
@@ -771,6 +824,16 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
     ps = srv.stats()
     srv.close()
     ctx.close()
+    classes = {}
+    for q, l in zip(pois_classes, lat):
+        classes.setdefault(q, []).append(l)
+    per_class = {}
+    for key in sorted(classes, key=lambda k: int(k.split("x")[0]) * int(k.split("x")[1])):
+        v = np.sort(np.asarray(classes[key]))
+        pm = plain_class_ms.get(key, [])
+        per_class[key] = {"requests": int(v.size), "p50_ms": float(np.percentile(v, 50)),
+                          "p99_ms": float(np.percentile(v, 99)),
+                          "plain_gpu_ms_mean": float(np.mean(pm)) if pm else None}
     return {
         "workload": f"Poisson {rate:.0f} req/s for {seconds:.0f} s; resolution {SERVE_RES} with p={SERVE_P}; "
                     f"{n_meshes} resident meshes of 5k..2M triangles (log-uniform, {sum(ntris) / 1e6:.1f}M total), "
@@ -782,7 +845,7 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
         "offered_rps": n / arrivals[-1], "achieved_frames_per_s": n / total_span, "submit_span_s": submit_span,
         "p50_ms": ps["p50_ms"], "p99_ms": ps["p99_ms"], "max_ms": ps["max_ms"],
         "p99_over_p50": ps["p99_ms"] / ps["p50_ms"] if ps["p50_ms"] else None, "mean_batch": ps["mean_batch"],
-        "peak_gib": ps["peak_bytes"] / 2**30, "errors": ps["error"],
+        "peak_gib": ps["peak_bytes"] / 2**30, "errors": ps["error"], "per_class": per_class,
     }
 
 

@@ -1,4 +1,11 @@
-"""Builds the in-tree CUDA library draw_gb300/_lib/libdrawgpu.so for sm_103a.
+"""Builds the in-tree CUDA library for sm_103a: draw_gb300/_lib/libdrawgpu.so
+(what the Python package and the tests load) and draw_gb300/_lib/libdrawgpu.a
+(the same objects as a static archive, for a host program that links the
+library statically, e.g. a Rust crate's build.rs). build(checked=True) makes
+draw_gb300/_lib/libdrawgpu_checked.so instead: compiled with DRAW_CHECKED, its
+kernels test the indices of their gathers and scatters against the buffers'
+sizes and record DG_E_CUDA in the error word, skipping the access, where one is
+out of range.
 
 Floating-point flags are part of the contract with the reference's Rust
 semantics: -fmad=false (no FMA contraction on the device), IEEE division and
@@ -18,6 +25,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
+ARCHIVE = os.path.join(LIBDIR, "libdrawgpu.a")
+CHECKED_LIB = os.path.join(LIBDIR, "libdrawgpu_checked.so")
 SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu", "dg_transparent.cu",
            "dg_selfcheck.cu", "dg_loader.cpp"]
 HEADERS = ["dg_internal.cuh", "dg_host.h", "dg_device.cuh"]
@@ -35,27 +44,29 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the draw_gb300 CUDA library cannot be built")
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
+def _stale(lib: str = LIB) -> bool:
+    if not os.path.exists(lib) or (lib == LIB and not os.path.exists(ARCHIVE)):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS]
     deps.append(os.path.join(HERE, "..", "include", "draw_gpu.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force: bool = False, verbose: bool = False, extra: list | None = None) -> str:
-    if not force and not _stale():
-        return LIB
+def build(force: bool = False, verbose: bool = False, extra: list | None = None, checked: bool = False) -> str:
+    lib = CHECKED_LIB if checked else LIB
+    if not force and not _stale(lib):
+        return lib
     os.makedirs(LIBDIR, exist_ok=True)
-    tag = f"{os.getpid()}"
+    tag = f"{os.getpid()}{'c' if checked else ''}"
+    extra = list(extra or []) + (["-DDRAW_CHECKED"] if checked else [])
     objs = []
     cmds = []
     for s in SOURCES:
         obj = os.path.join(LIBDIR, os.path.splitext(s)[0] + f".{tag}.o")
         objs.append(obj)
-        cmds.append([nvcc(), *ARCH, *NVCC_FLAGS, *(extra or []), "-c", os.path.join(CSRC, s), "-o", obj])
+        cmds.append([nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, s), "-o", obj])
     with cf.ThreadPoolExecutor(len(cmds)) as ex:
         res = list(ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), cmds))
     for c, r in zip(cmds, res):
@@ -63,21 +74,28 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None)
             sys.stderr.write(" ".join(c) + "\n" + r.stdout + r.stderr)
         if r.returncode:
             raise RuntimeError(f"nvcc failed on {c[-3]}")
-    tmp = LIB + f".{tag}.tmp"
+    tmp = lib + f".{tag}.tmp"
     link = [nvcc(), *ARCH, "-shared", *objs, "-o", tmp]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode:
         sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)
         raise RuntimeError("nvcc link failed")
-    os.replace(tmp, LIB)
+    if not checked:
+        atmp = ARCHIVE + f".{tag}.tmp.a"
+        r = subprocess.run(["ar", "rcs", atmp, *objs], capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(r.stdout + r.stderr)
+            raise RuntimeError("ar failed")
+        os.replace(atmp, ARCHIVE)
+    os.replace(tmp, lib)
     for o in objs:
         try:
             os.remove(o)
         except OSError:
             pass
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
-                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None))
+                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None, checked="--checked" in sys.argv))

@@ -696,6 +696,9 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.rec_of = S.d_rec_of;
     job.trec = S.d_trec;
     job.trec_w = any_persp ? S.d_trec_w : nullptr;
+    job.ext = any_persp ? 1u : 0u;
+    for (const TexMap& t : c->tex)
+        if (t.filter != DG_FILTER_NEAREST) job.ext = 1u;
     job.ttrec_w = any_persp && ntt ? S.d_ttrec_w : nullptr;
     job.trec_cap = (uint32_t)std::min<size_t>(S.trec_cap, 0xFFFFFFF0ull);
     if (S.record_limit) job.trec_cap = std::min(job.trec_cap, S.record_limit);
@@ -766,7 +769,8 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
 dg_status enqueue_job(JobBuild& B, JobSlot& S, void* d_stage, cudaStream_t stream, bool timing) {
     B.job.frames = (const DgFrameDev*)d_stage;
     B.job.segs = (const DgSegDev*)((uint8_t*)d_stage + B.fbytes);
-    DG_CUDA(cudaMemsetAsync(S.d_counters, 0, DG_NCOUNTERS * sizeof(unsigned long long), stream));
+    if (!B.job.total_vtx)  // otherwise the first kernel zeroes them
+        DG_CUDA(cudaMemsetAsync(S.d_counters, 0, DG_NCOUNTERS * sizeof(unsigned long long), stream));
     DG_CUDA(dg_launch_job(B.job, B.cfg, stream, timing ? S.ev : nullptr));
     return DG_OK;
 }
@@ -796,9 +800,21 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
         if (e) return e;
         S.stage_cap[k] = cap;
     }
-    std::memcpy(S.h_stage[k], B.frames.data(), B.fbytes);
-    std::memcpy((uint8_t*)S.h_stage[k] + B.fbytes, B.segs.data(), B.sbytes);
-    DG_CUDA(cudaMemcpyAsync(S.d_stage[k], S.h_stage[k], need, cudaMemcpyHostToDevice, S.stream));
+    // A small job's descriptors go to the device as a kernel parameter (k_vertex
+    // writes them to the staging buffer); larger ones are copied.
+    DgInlineDesc inl;
+    const bool inline_desc = B.frames.size() == 1 && B.segs.size() <= DG_INLINE_SEGS && B.total_vtx > 0;
+    if (inline_desc) {
+        std::memset(&inl, 0, sizeof(inl));
+        inl.frame = B.frames[0];
+        for (size_t i = 0; i < B.segs.size(); i++) inl.segs[i] = B.segs[i];
+        inl.nsegs = (uint32_t)B.segs.size();
+        B.cfg.inl = &inl;
+    } else {
+        std::memcpy(S.h_stage[k], B.frames.data(), B.fbytes);
+        std::memcpy((uint8_t*)S.h_stage[k] + B.fbytes, B.segs.data(), B.sbytes);
+        DG_CUDA(cudaMemcpyAsync(S.d_stage[k], S.h_stage[k], need, cudaMemcpyHostToDevice, S.stream));
+    }
     DG_CUDA(cudaEventRecord(S.stage_ev[k], S.stream));
     S.last_vtx = B.total_vtx;
     S.last_tri = B.total_tri;
@@ -842,6 +858,7 @@ const char* dg_status_string(dg_status s) {
         case DG_E_OOM: return "out of device memory";
         case DG_E_LIMIT: return "size or feature beyond a documented limit";
         case DG_E_TIMEOUT: return "bounded wait timed out";
+        case DG_E_CANCELLED: return "request cancelled";
         default: return "unknown status";
     }
 }

@@ -160,6 +160,10 @@ __device__ __forceinline__ float4 vertex_screen(const DgFrameDev& fr, float4 p4,
 __device__ __forceinline__ void triangle_vertices(const DgJobDev& job, const DgSegDev& sg, const DgFrameDev& fr,
                                                   uint4 tp, float4 r[3]) {
     (void)fr;
+    if (!DG_IN_RANGE(tp.x < sg.nv && tp.y < sg.nv && tp.z < sg.nv, job.err)) {
+        r[0] = r[1] = r[2] = make_float4(NAN, NAN, NAN, 0.0f);  // no plane bit: the triangle is dropped
+        return;
+    }
     r[0] = __ldg(job.vrec + sg.vtx_begin + tp.x);
     r[1] = __ldg(job.vrec + sg.vtx_begin + tp.y);
     r[2] = __ldg(job.vrec + sg.vtx_begin + tp.z);
@@ -762,8 +766,10 @@ struct MatVals {
 
 // Shading of canvas.rs:713-741 from the interpolated texture coordinates,
 // normal and per-light vectors: lv(l, lt, h) gives the interpolated light and
-// halfway vectors of light l.
-template <class LV>
+// halfway vectors of light l. EXT: the texture maps may use the bilinear
+// extension (false compiles the reference's nearest fetch alone, which keeps
+// the extension's out-of-line call and its register spills off that path).
+template <bool EXT, class LV>
 __device__ __forceinline__ uint32_t shade_colour(const DgJobDev& job, const DgTexDev* stex, const DgFrameDev& fr,
                                                  const MatVals& m, float pu, float pv, V3 pn, const float* inv255,
                                                  int& errc, LV lv) {
@@ -784,7 +790,7 @@ __device__ __forceinline__ uint32_t shade_colour(const DgJobDev& job, const DgTe
     // Pixel::normalized_as_vec3 (canvas.rs:81-87): byte / 255.0, looked up in a
     // table of the 256 correctly rounded quotients; or the bilinear extension
     auto sample = [&](const DgTexDev& t, V3& out) -> bool {
-        if (t.filter == DG_FILTER_BILINEAR) return tex_bilinear(t, pu, pv, inv255, out);
+        if (EXT && t.filter == DG_FILTER_BILINEAR) return tex_bilinear(t, pu, pv, inv255, out);
         uint32_t rgb = 0;
         if (!tex_rgb(t, pu, pv, rgb)) return false;
         out = V3{inv255[rgb & 0xFFu], inv255[(rgb >> 8) & 0xFFu], inv255[(rgb >> 16) & 0xFFu]};
@@ -838,7 +844,9 @@ __device__ __forceinline__ const float4* shade_row(const DgJobDev& job, uint32_t
 
 // Shades the winning fragment of pixel (x, y) from its triangle record:
 // canvas.rs:682-741.
-// Wp (frames with DG_FRAME_PERSPECTIVE, else null): the record's inv_w3.
+// Wp (frames with DG_FRAME_PERSPECTIVE, else null): the record's inv_w3. EXT
+// as for shade_colour (false: the reference's interpolation and fetch only).
+template <bool EXT>
 __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const DgFrameDev& fr, const DgTriRec* R,
                                                       uint32_t x, uint32_t y, const float* inv255,
                                                       const DgTexDev* stex, float& depth_out, int& errc,
@@ -856,7 +864,7 @@ __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const
     float be = fD(edge_eval(e, 1, xf, yf), e.den[1]);
     float ga = fD(edge_eval(e, 2, xf, yf), e.den[2]);
     depth_out = interp(al, be, ga, dd.x, dd.y, dd.z);
-    if (Wp) persp_weights(al, be, ga, __ldg(Wp));  // coverage and depth keep the screen-space weights
+    if (EXT && Wp) persp_weights(al, be, ga, __ldg(Wp));  // coverage and depth keep the screen-space weights
     const float pu = interp(al, be, ga, fu.x, fu.y, fu.z);
     const float pv = interp(al, be, ga, fv.x, fv.y, fv.z);
     const V3 pn = {interp(al, be, ga, fx.x, fx.y, fx.z), interp(al, be, ga, fy.x, fy.y, fy.z),
@@ -868,6 +876,13 @@ __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const
     m.map_ka = last.z;
     m.map_kd = last.w;
     auto lv = [&](uint32_t l, V3& lt, V3& h) {
+        if (DG_CHECKED) {
+            const uint32_t nrow = job.total_vtx + job.vrow_extra + 6u * job.ntt;
+            if (!DG_IN_RANGE(rows.x < nrow && rows.y < nrow && rows.z < nrow, job.err)) {
+                lt = h = V3{0.0f, 0.0f, 0.0f};
+                return;
+            }
+        }
         const float4* pa = shade_row(job, rows.x, l);
         const float4* pb = shade_row(job, rows.y, l);
         const float4* pc = shade_row(job, rows.z, l);
@@ -878,7 +893,7 @@ __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const
         h = V3{interp(al, be, ga, a.w, b.w, c.w), interp(al, be, ga, a1.x, b1.x, c1.x),
                interp(al, be, ga, a1.y, b1.y, c1.y)};
     };
-    return shade_colour(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
+    return shade_colour<EXT>(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
 }
 
 // Shades the winning fragment of pixel (x, y) from its key alone (the triangle
@@ -986,7 +1001,7 @@ __device__ __noinline__ uint32_t shade_without_record(const DgJobDev& job, const
         lt = V3{comp(l, 0), comp(l, 1), comp(l, 2)};
         h = V3{comp(l, 3), comp(l, 4), comp(l, 5)};
     };
-    return shade_colour(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
+    return shade_colour<true>(job, stex, fr, m, pu, pv, pn, inv255, errc, lv);
 }
 
 inline unsigned grid_for(uint64_t n, unsigned cap) {

@@ -22,6 +22,23 @@
 #include "../../include/draw_gpu.h"
 
 #define DG_MAXL DG_MAX_LIGHTS
+
+// DRAW_CHECKED builds (draw_gb300/_build.py build(checked=True)): the kernels
+// test the data-dependent indices of their gathers and scatters (mesh indices,
+// queue entries, light/halfway rows, raster boxes) against the buffers' sizes;
+// an index out of range records DG_E_CUDA in the job's error word and the
+// access is skipped. Off in the normal build, where the host validates the
+// indices and the kernels' own arithmetic keeps the rest in range.
+#ifdef DRAW_CHECKED
+#define DG_CHECKED 1
+#else
+#define DG_CHECKED 0
+#endif
+#define DG_IN_RANGE(cond, err) (!DG_CHECKED || dg_check_range((cond), (err)))
+__device__ __forceinline__ bool dg_check_range(bool ok, uint32_t* err) {
+    if (!ok) atomicOr(err, 1u << 6 /* DG_E_CUDA */);
+    return ok;
+}
 #define DG_VIS_EMPTY 0xFFFFFFFFFFFFFFFFull
 
 // Triangles whose clipped bounding box has at most this many pixels go to the
@@ -204,6 +221,7 @@ struct DgJobDev {
     // no frame of the job has it). ttrec_w: the same for ttrec.
     float4* trec_w;
     float4* ttrec_w;
+    uint32_t ext;  // 1: a frame uses perspective-correct interpolation or a texture map the bilinear filter
     uint32_t trec_cap;
     uint32_t queue_cap;
     DgQueueRec* queue;
@@ -245,11 +263,24 @@ struct DgTransparentPlan {
     unsigned blocks;                   // grid of the grid-stride kernels
 };
 
+// The descriptors of a small job (one frame, at most DG_INLINE_SEGS segments)
+// travel as a kernel parameter of k_vertex instead of a host-to-device copy:
+// k_vertex reads them from its parameter and writes them to job.frames and
+// job.segs, where the later kernels of the job read them.
+#define DG_INLINE_SEGS 4
+struct alignas(16) DgInlineDesc {
+    DgFrameDev frame;
+    DgSegDev segs[DG_INLINE_SEGS];
+    uint32_t nsegs;  // 0: the descriptors were copied to the device by the host
+    uint32_t pad[3];
+};
+
 // Host-side launchers (dg_kernels.cu).
 struct DgLaunchCfg {
     unsigned cull_blocks;   // grid caps / sizes in 256-thread blocks
     unsigned setup_blocks;
     unsigned queue_blocks;
+    const DgInlineDesc* inl;  // host memory, read at launch; null: descriptors already on the device
     DgTransparentPlan tplan;
 };
 #define DG_SETUP_BLOCKS_PER_SM 4u
@@ -259,7 +290,9 @@ struct DgLaunchCfg {
 #define DG_NKERNELS 5  // vertex, cull, setup_raster, queue_raster, resolve (+ the transparent pass)
 #define DG_SORT_TILE 4096u  // keys per radix-sort tile (256 threads x 16)
 // Launches the whole pipeline of one job on stream s. ev, if not null, holds
-// DG_NKERNELS + 1 events recorded around the kernels (per-kernel timing).
+// DG_NKERNELS + 1 events recorded around the kernels (per-kernel timing). The
+// first kernel zeroes the job counters when the job has vertices; the caller
+// zeroes them otherwise.
 cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev);
 // The transparent pass (dg_transparent.cu), in three parts launched by
 // dg_launch_job: part 0 after the opaque setup (painter's sort, gather,

@@ -33,18 +33,23 @@
 // saturating float->int casts, and wrapping usize arithmetic for texel offsets.
 #include "dg_device.cuh"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace {
 
 // ================================================================ kernels
 // Each pass is a device function over the whole grid (grid-stride or
 // block-uniform loops) wrapped by its kernel; the five kernels run as a chain
 // with programmatic dependent launch.
-__device__ __forceinline__ void dev_vertex(const DgJobDev& job) {
+// seg(i) and frame(i) give the job's descriptors (from global memory, or from
+// k_vertex's parameter for a small job).
+template <class SEG, class FRM>
+__device__ __forceinline__ void dev_vertex(const DgJobDev& job, uint32_t nsegs, SEG seg, FRM frame) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < job.total_vtx; v += stride) {
-        uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
-        const DgSegDev& sg = job.segs[si];
-        const DgFrameDev& fr = job.frames[sg.frame];
+        uint32_t si = last_le(nsegs, v, [&](uint32_t i) { return seg(i).vtx_begin; });
+        const DgSegDev& sg = seg(si);
+        const DgFrameDev& fr = frame(sg.frame);
         float4 p4 = __ldg(sg.pos + (v - sg.vtx_begin));
         V3 p = {p4.x, p4.y, p4.z};
         uint32_t mask = 0;
@@ -59,9 +64,35 @@ __device__ __forceinline__ void dev_vertex(const DgJobDev& job) {
     }
 }
 
-__global__ void __launch_bounds__(256, 8) k_vertex(const DgJobDev job) {
+// Also zeroes the job counters (the later kernels read them only after waiting
+// for this one) and, for a small job, writes the descriptors of its parameter
+// `in` to job.frames and job.segs.
+__global__ void __launch_bounds__(256, 8) k_vertex(const __grid_constant__ DgJobDev job,
+                                                   const __grid_constant__ DgInlineDesc in) {
     allow_next_kernel();
-    dev_vertex(job);
+    if (blockIdx.x == 0) {
+        if (threadIdx.x < DG_NCOUNTERS) job.cnt[threadIdx.x] = 0ull;
+        if (in.nsegs) {
+            constexpr uint32_t fw = sizeof(DgFrameDev) / 8, sw = sizeof(DgSegDev) / 8;
+            static_assert(sizeof(DgFrameDev) % 8 == 0 && sizeof(DgSegDev) % 8 == 0, "8-byte words");
+            uint2* fd = reinterpret_cast<uint2*>(const_cast<DgFrameDev*>(job.frames));
+            uint2* sd = reinterpret_cast<uint2*>(const_cast<DgSegDev*>(job.segs));
+            const uint2* fs = reinterpret_cast<const uint2*>(&in.frame);
+            const uint2* ss = reinterpret_cast<const uint2*>(in.segs);
+            for (uint32_t i = threadIdx.x; i < fw + in.nsegs * sw; i += blockDim.x) {
+                if (i < fw)
+                    fd[i] = fs[i];
+                else
+                    sd[i - fw] = ss[i - fw];
+            }
+        }
+    }
+    if (in.nsegs)
+        dev_vertex(job, in.nsegs, [&](uint32_t i) -> const DgSegDev& { return in.segs[i]; },
+                   [&](uint32_t) -> const DgFrameDev& { return in.frame; });
+    else
+        dev_vertex(job, job.nsegs, [&](uint32_t i) -> const DgSegDev& { return job.segs[i]; },
+                   [&](uint32_t i) -> const DgFrameDev& { return job.frames[i]; });
 }
 
 
@@ -87,7 +118,9 @@ __device__ __forceinline__ void dev_cull(const DgJobDev& job) {
             const DgSegDev& sg = job.segs[si];
             const uint4 tp = __ldg(sg.tri_pos + (g - sg.tri_begin));
             const uint16_t* vm = job.vmask + sg.vtx_begin;
-            const uint32_t m = (uint32_t)__ldg(vm + tp.x) & (uint32_t)__ldg(vm + tp.y) & (uint32_t)__ldg(vm + tp.z);
+            const bool ok = DG_IN_RANGE(tp.x < sg.nv && tp.y < sg.nv && tp.z < sg.nv, job.err);
+            const uint32_t m = ok ? (uint32_t)__ldg(vm + tp.x) & (uint32_t)__ldg(vm + tp.y) & (uint32_t)__ldg(vm + tp.z)
+                                  : 0xFFFFu;
             if (((m >> 8) & 0x3Du) == 0u) {
                 const float4 pa = __ldg(sg.pos + tp.x), pb = __ldg(sg.pos + tp.y), pc = __ldg(sg.pos + tp.z);
                 const V3 a = {pa.x, pa.y, pa.z}, b = {pb.x, pb.y, pb.z}, c = {pc.x, pc.y, pc.z};
@@ -458,9 +491,15 @@ __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
 // clear depth and the keyed minimum.
 // rcp (uniform over the warp): the edge set passed edge_rcp_ok and yr holds the
 // reciprocals of its three dens.
-__device__ __forceinline__ void finish_fragment(const EdgeSet& e, float4 dd, uint32_t seq, uint32_t x, uint32_t y,
+// The edge set and the vertex depths are read from the record R (cached: every
+// call of a work item reads the same words), which keeps them out of the unit
+// loop's registers.
+__device__ __forceinline__ void finish_fragment(const DgTriRec* R, uint32_t seq, uint32_t x, uint32_t y,
                                                 float clear_depth, unsigned long long* vis, uint32_t width, bool rcp,
                                                 float3 yr) {
+    EdgeSet e;
+    load_edges(R, e);
+    const float4 dd = __ldg(reinterpret_cast<const float4*>(R) + 4);
     float al, be, ga;
     const float xf = (float)x, yf = (float)y;
     const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
@@ -575,13 +614,15 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
         const DgTriRec* R = job.trec + q0.x;
         EdgeSet e;
         load_edges(R, e);
-        const float4 dd = __ldg(reinterpret_cast<const float4*>(R) + 4);
         const uint32_t seq = q0.y;
         const DgFrameDev& fr = job.frames[q0.z];
         const float clear_depth = fr.clear_depth;
         unsigned long long* vis = reinterpret_cast<unsigned long long*>(fr.vis);
         const uint32_t width = fr.width;
         const uint32_t xlo = q0.w, ylo = q1.x, w = q1.y, npx = q1.z;
+        if (!DG_IN_RANGE(w != 0u && xlo + w <= width && ylo + (npx + w - 1u) / w <= fr.height && q0.x < job.trec_cap,
+                         job.err))
+            continue;
         const uint32_t u_end = min(q1.w, item.y + job.item_units);
         // Stage A: every lane takes one pixel of the unit and applies the exact,
         // division-free pre-reject; candidates are packed into the warp's buffer.
@@ -599,21 +640,8 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
         uint32_t k = item.y * DG_UNIT_PX + lane;
         uint32_t yy = k / w, xx = k - yy * w;
         const uint32_t q32 = DG_UNIT_PX / w, r32 = DG_UNIT_PX - q32 * w;
-        for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
-            bool cand = false;
-            const uint32_t x = xlo + xx, y = ylo + yy;
-            xx += r32;
-            yy += q32;
-            if (xx >= w) {
-                xx -= w;
-                yy++;
-            }
-            if (k < npx) {
-                const float xf = (float)x, yf = (float)y;
-                const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
-                cand = fast ? covered_signs(e.tie, n0, n1, n2)
-                            : !(prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2]));
-            }
+        // Buffers this unit's candidates and finishes 32 whenever that many are buffered.
+        auto push = [&](bool cand, uint32_t x, uint32_t y) {
             const unsigned b = __ballot_sync(FULL, cand);
             if (cand) {
                 const uint32_t slot = pending + __popc(b & ((1u << lane) - 1u));
@@ -623,7 +651,7 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
             pending += __popc(b);
             if (pending >= 32u) {
                 __syncwarp();
-                finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);
+                finish_fragment(R, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);
                 __syncwarp();
                 if (lane < pending - 32u) {
                     bx[lane] = bx[32u + lane];
@@ -632,9 +660,71 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
                 __syncwarp();
                 pending -= 32u;
             }
+        };
+        // Exact stepping (fast edge sets whose box is small enough): when every
+        // term of every edge value over the box, |A| x + |B| y + |C| + |D| with
+        // the step of a unit included, stays below 2^24, all of them are integers
+        // that f32 holds exactly, so the reference's per-pixel expression equals
+        // the exact linear function, and a lane advances its three values by the
+        // exact change of one unit (A r32 + B q32, or with the carry into the next
+        // row A (r32 - w) + B (q32 + 1)) instead of evaluating them again. The
+        // coverage test on integer values is a comparison with -1/2 (tie edge:
+        // n >= 0) or 1/2 (n > 0).
+        bool exact = fast;
+        if (fast) {
+            const float X = (float)(xlo + w), Y = (float)(ylo + (npx + w - 1u) / w + DG_UNIT_PX + 1u);
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const float S = fA(fA(fA(fM(fabsf(e.A[j]), X), fM(fabsf(e.B[j]), Y)), fabsf(e.C[j])), fabsf(e.D[j]));
+                exact = exact && S < 16000000.0f;
+            }
+        }
+        if (exact) {
+            const float x0 = (float)(xlo + xx), y0 = (float)(ylo + yy);
+            float n0 = edge_eval(e, 0, x0, y0), n1 = edge_eval(e, 1, x0, y0), n2 = edge_eval(e, 2, x0, y0);
+            const float fr32 = (float)r32, fq32 = (float)q32;
+            const float frc = -(float)(w - r32), fqc = (float)(q32 + 1u);
+            const float dq0 = fA(fM(e.A[0], fr32), fM(e.B[0], fq32)), dc0 = fA(fM(e.A[0], frc), fM(e.B[0], fqc));
+            const float dq1 = fA(fM(e.A[1], fr32), fM(e.B[1], fq32)), dc1 = fA(fM(e.A[1], frc), fM(e.B[1], fqc));
+            const float dq2 = fA(fM(e.A[2], fr32), fM(e.B[2], fq32)), dc2 = fA(fM(e.A[2], frc), fM(e.B[2], fqc));
+            const float th0 = (e.tie & 1u) ? -0.5f : 0.5f, th1 = (e.tie & 2u) ? -0.5f : 0.5f,
+                        th2 = (e.tie & 4u) ? -0.5f : 0.5f;
+            for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
+                const uint32_t x = xlo + xx, y = ylo + yy;
+                const bool cand = k < npx && n0 > th0 && n1 > th1 && n2 > th2;
+                xx += r32;
+                yy += q32;
+                const bool carry = xx >= w;
+                if (carry) {
+                    xx -= w;
+                    yy++;
+                }
+                n0 = fA(n0, carry ? dc0 : dq0);
+                n1 = fA(n1, carry ? dc1 : dq1);
+                n2 = fA(n2, carry ? dc2 : dq2);
+                push(cand, x, y);
+            }
+        } else {
+            for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
+                bool cand = false;
+                const uint32_t x = xlo + xx, y = ylo + yy;
+                xx += r32;
+                yy += q32;
+                if (xx >= w) {
+                    xx -= w;
+                    yy++;
+                }
+                if (k < npx) {
+                    const float xf = (float)x, yf = (float)y;
+                    const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
+                    cand = fast ? covered_signs(e.tie, n0, n1, n2)
+                                : !(prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2]));
+                }
+                push(cand, x, y);
+            }
         }
         __syncwarp();
-        if (lane < pending) finish_fragment(e, dd, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);
+        if (lane < pending) finish_fragment(R, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);
         __syncwarp();
     }
 }
@@ -706,8 +796,9 @@ __device__ __forceinline__ void resolve_prologue(const DgJobDev& job, float* inv
 }
 
 // One tile of the resolve pass (block-uniform; the tables of resolve_prologue
-// must be in place).
-template <uint32_t TH>
+// must be in place). EXT: the job uses an extension mode (perspective-correct
+// interpolation or bilinear fetch); false compiles the reference's shading only.
+template <uint32_t TH, bool EXT>
 __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint32_t tile, const float* inv255,
                                                  const DgTexDev* stex) {
     __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
@@ -724,6 +815,23 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
     if (fr.cells != nullptr && __ldcg(fr.cells + ((ty * TH) >> 5) * fr.tiles_x + tx) != fr.epoch) {
         // No triangle's box reached the tile's 32x32 cell this frame, so all its
         // keys are empty: the clear values, without reading the keys (block-uniform).
+        // 16-byte stores of four pixels where the rows are 16-byte aligned.
+        const uint32_t x0 = tx * DG_TILE_W;
+        const bool vec = (W & 3u) == 0u && x0 + DG_TILE_W <= W &&
+                         ((reinterpret_cast<uintptr_t>(fr.depth) | reinterpret_cast<uintptr_t>(fr.colour)) & 15u) == 0u;
+        if (vec) {
+            const uint32_t r = threadIdx.x >> 3, c = (threadIdx.x & 7u) * 4u;
+            const float cd = fr.clear_depth;
+            for (uint32_t yy = r; yy < TH; yy += 32u) {
+                const uint32_t y = ty * TH + yy;
+                if (y < H) {
+                    *reinterpret_cast<float4*>(fr.depth + (uint64_t)y * W + x0 + c) = make_float4(cd, cd, cd, cd);
+                    *reinterpret_cast<uint4*>(fr.colour + (uint64_t)(H - 1u - y) * W + x0 + c) =
+                        make_uint4(AZUL_BB, AZUL_BB, AZUL_BB, AZUL_BB);
+                }
+            }
+            return;
+        }
 #pragma unroll
         for (int j = 0; j < R; j++) {
             const uint32_t y = ty * TH + wid + 8u * j;
@@ -807,8 +915,8 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
         const uint32_t px = tx * DG_TILE_W + (pe & 31u), py = ty * TH + (pe >> 5);
         float d = 0.0f;
         int errc;
-        const float4* wp = (fr.flags & DG_FRAME_PERSPECTIVE) && job.trec_w ? job.trec_w + s_val[k] : nullptr;
-        uint32_t c = shade_from_record(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc, wp);
+        const float4* wp = EXT && (fr.flags & DG_FRAME_PERSPECTIVE) && job.trec_w ? job.trec_w + s_val[k] : nullptr;
+        uint32_t c = shade_from_record<EXT>(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc, wp);
         if (errc != DG_OK) c = AZUL_BB;
         // one error-word update per warp (every pixel of a bad job may fail)
         const unsigned act = __activemask();
@@ -821,13 +929,13 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
     if (any_no_record) shade_tile_without_records<TH>(job, tile, inv255, stex);
 }
 
-template <uint32_t TH>
+template <uint32_t TH, bool EXT>
 __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
     __shared__ float inv255[256];
     __shared__ DgTexDev stex[DG_SMEM_TEX];
     resolve_prologue(job, inv255, stex);
     wait_previous_kernel();
-    dev_resolve_tile<TH>(job, blockIdx.x, inv255, stex);
+    dev_resolve_tile<TH, EXT>(job, blockIdx.x, inv255, stex);
 }
 
 __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, float dv, int fc, int fd) {
@@ -853,21 +961,34 @@ __global__ void k_vis_reset(uint64_t* vis, uint64_t n) {
 
 }  // namespace
 
+// NVTX ranges name each pass's launch on a profiler's timeline (nvtx3 is
+// header-only; without an attached tool a range costs a branch).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev) {
+    NvtxRange job_range("draw_gb300 render job");
     cudaError_t e;
     auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
     if ((e = mark(0)) != cudaSuccess) return e;
     if (job.total_vtx) {
-        k_vertex<<<grid_for(job.total_vtx, 1u << 20), 256, 0, s>>>(job);
+        NvtxRange r("k_vertex");
+        DgInlineDesc none;
+        if (!cfg.inl) none.nsegs = 0;
+        k_vertex<<<grid_for(job.total_vtx, 1u << 20), 256, 0, s>>>(job, cfg.inl ? *cfg.inl : none);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if ((e = mark(1)) != cudaSuccess) return e;
     if (job.total_tri) {
+        NvtxRange r("k_cull");
         const unsigned cb = cfg.cull_blocks < 1u ? 1u : cfg.cull_blocks;
         if ((e = launch_dependent(k_cull, grid_for(job.total_tri, cb), 256, job, s)) != cudaSuccess) return e;
     }
     if ((e = mark(2)) != cudaSuccess) return e;
     if (job.total_tri) {
+        NvtxRange r("k_setup_raster");
         const unsigned sb = cfg.setup_blocks < 1u ? 1u : cfg.setup_blocks;
         if ((e = launch_dependent(k_setup_raster, grid_for(job.total_tri, sb), 256, job, s)) != cudaSuccess) return e;
     }
@@ -876,6 +997,7 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
     // lighting prologue of the queue pass)
     if ((e = dg_launch_transparent(0, job, cfg.tplan, s)) != cudaSuccess) return e;
     if (job.total_tri || job.ntt) {
+        NvtxRange r("k_queue_raster");
         const unsigned qb = cfg.queue_blocks < 1u ? 1u : cfg.queue_blocks;
         if ((e = launch_dependent(k_queue_raster, qb, 256, job, s)) != cudaSuccess) return e;
     }
@@ -883,7 +1005,11 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
     // part 1: transparent fragments, read against the opaque winners' keys
     if ((e = dg_launch_transparent(1, job, cfg.tplan, s)) != cudaSuccess) return e;
     if (job.total_tiles) {
-        auto kr = job.tile_rows == 8u ? k_resolve<8> : job.tile_rows == 16u ? k_resolve<16> : k_resolve<32>;
+        NvtxRange r("k_resolve");
+        auto kr = job.ext ? (job.tile_rows == 8u ? k_resolve<8, true> : job.tile_rows == 16u ? k_resolve<16, true>
+                                                                                         : k_resolve<32, true>)
+                          : (job.tile_rows == 8u ? k_resolve<8, false> : job.tile_rows == 16u ? k_resolve<16, false>
+                                                                                              : k_resolve<32, false>);
         if ((e = launch_dependent(kr, job.total_tiles, 256, job, s)) != cudaSuccess) return e;
     }
     // part 2: the ordered blend over the opaque colours

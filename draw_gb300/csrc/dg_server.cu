@@ -1,14 +1,24 @@
 // dg_server.cu -- a continuous-batching render server on one GPU.
 //
 // Clients submit render requests (a resident object, a frame size, a camera,
-// lights) from any thread. A scheduler thread admits pending requests in
-// arrival order while the device-memory budget allows (each request holds its
-// own colour, depth and visibility buffers; job-slot scratch counts too),
-// packs up to max_batch of them into one render job, and launches it on a free
-// job slot (its own stream and scratch). Several batches are in flight at
-// once, so requests that arrive while others run are admitted as soon as a
-// slot and memory free up, and their work overlaps on the device. A host
-// callback on the slot's stream stamps each request's completion time.
+// lights) from any thread. Requests go to one of two lanes: large ones (at
+// least 1920x1080 pixels or 1M triangles) and the rest, each lane with its own
+// arrival-ordered queue and its own job slots (stream and scratch), so a small
+// request never waits behind a large frame. A scheduler thread admits pending
+// requests of a lane in arrival order while the device-memory budget allows
+// (each request holds colour, depth and visibility buffers; job-slot scratch
+// counts too), packs up to max_batch of them (large lane: at most
+// kLargeBatch) into one render job, and launches it on a free slot of the lane.
+// Several batches are in flight at once, so requests that arrive while others
+// run are admitted as soon as a slot and memory free up, and their work
+// overlaps on the device. A host callback on the slot's stream stamps each
+// request's completion time.
+//
+// Request buffers are pooled per frame size: a finished request's buffers go
+// back to the pool (their visibility keys are all empty again: the resolve
+// pass resets every key it reads), so a later request of that size takes them
+// without an allocation or a clear. Pooled buffers count against the budget;
+// when a request does not fit, pooled buffers of other sizes are released.
 //
 // Every request renders exactly as dg_scene_render would render it alone: a
 // batch is the same kernels over more frames, with per-frame keys and buffers.
@@ -35,21 +45,30 @@ double now_s() {
 
 enum ReqState { kPending = 0, kRunning = 1, kDone = 2 };
 
+constexpr int kLanes = 2;            // 0: small requests, 1: large ones
+constexpr uint32_t kLargeBatch = 4;  // requests per batch in the large lane
+constexpr uint64_t kLargePixels = 1920ull * 1080ull;
+constexpr uint64_t kLargeTris = 1000000ull;
+
 struct Request {
     uint64_t ticket = 0;
     Scene scene;
     FrameTarget tgt{};
-    void* mem = nullptr;  // one allocation: vis | colour | depth | cells
+    void* mem = nullptr;  // one buffer set: vis | colour | depth | cells
     uint64_t bytes = 0;
+    uint64_t size_key = 0;  // (width << 32) | height: the buffer pool of the request's size
+    int lane = 0;
     double t_submit = 0, t_start = 0, t_done = 0;
     int state = kPending;
     dg_status status = DG_OK;
     bool discard = false;
+    bool fail_alloc = false;  // dg_server_inject_alloc_failure
 };
 
 struct Slot {
     JobSlot js;
     bool busy = false;
+    int lane = 0;
     std::vector<Request*> batch;
     uint32_t* h_err = nullptr;  // pinned copy of the slot's error word
     struct dg_server* srv = nullptr;
@@ -65,9 +84,12 @@ struct dg_server {
     uint64_t held_done = 0;  // buffers of finished requests not yet collected by dg_server_wait
     uint32_t max_batch = 1;
     std::vector<std::unique_ptr<Slot>> slots;
-    std::deque<Request*> pending;
+    std::deque<Request*> pending[kLanes];
     std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
-    std::vector<void*> to_free;  // buffers of finished discard requests, freed by the scheduler
+    // buffers back from finished requests, by frame size (counted in `used`)
+    std::unordered_map<uint64_t, std::vector<void*>> pool;
+    uint64_t pooled_bytes = 0;
+    std::vector<void*> to_free;  // buffers the scheduler releases to the device
     std::vector<uint64_t> to_free_bytes;
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
@@ -76,6 +98,7 @@ struct dg_server {
     uint64_t next_ticket = 1;
     std::vector<double> latencies_ms;
     uint64_t batches = 0, frames = 0;
+    uint64_t allocations = 0;  // buffer sets allocated (the others came from the pool)
     dg_status sticky = DG_OK;  // first launch error, reported by later calls
     cudaStream_t copy_stream = nullptr;
 };
@@ -83,6 +106,13 @@ struct dg_server {
 namespace {
 
 uint64_t request_bytes(uint64_t w, uint64_t h) { return w * h * (4 + 4 + 8) + dg_cell_count(w, h) * 4; }
+
+// A finished request's buffers go back to the pool of its size (lock held).
+void pool_put(dg_server* s, Request* r) {
+    s->pool[r->size_key].push_back(r->mem);
+    s->pooled_bytes += r->bytes;
+    r->mem = nullptr;
+}
 
 // Host callback at the end of a batch on its slot stream (no CUDA calls allowed here).
 void CUDART_CB batch_done(void* arg) {
@@ -102,9 +132,13 @@ void CUDART_CB batch_done(void* arg) {
         r->status = st;
         s->latencies_ms.push_back((r->t_done - r->t_submit) * 1e3);
         if (r->discard) {
-            s->to_free.push_back(r->mem);
-            s->to_free_bytes.push_back(r->bytes);
-            r->mem = nullptr;
+            if (st == DG_OK) {
+                pool_put(s, r);
+            } else {  // keys may be left set: the buffers are released, not pooled
+                s->to_free.push_back(r->mem);
+                s->to_free_bytes.push_back(r->bytes);
+                r->mem = nullptr;
+            }
         } else {
             s->held_done += r->bytes;  // kept until the client collects the frame
         }
@@ -116,7 +150,10 @@ void CUDART_CB batch_done(void* arg) {
     s->cv_done.notify_all();
 }
 
-// Launches one batch on slot sl (called by the scheduler without the lock held).
+// Launches one batch on slot sl (called by the scheduler without the lock
+// held). Each request takes a pooled buffer set of its size or allocates one
+// (a fresh set has its visibility keys cleared once). A request whose
+// allocation fails completes alone with DG_E_OOM; the others still render.
 dg_status launch_batch(dg_server* s, Slot* sl, std::vector<Request*>& batch, uint64_t reserved) {
     cudaStream_t st = sl->js.stream;
     const uint64_t scratch_before = sl->js.scratch_bytes;
@@ -126,13 +163,31 @@ dg_status launch_batch(dg_server* s, Slot* sl, std::vector<Request*>& batch, uin
         s->used = s->used - reserved + (sl->js.scratch_bytes - scratch_before);
         s->peak_used = std::max(s->peak_used, s->used);
     };
+    std::vector<Request*> run;
     for (Request* r : batch) {
         const uint64_t n = r->scene.width * r->scene.height;
-        if (cudaMallocAsync(&r->mem, r->bytes, st) != cudaSuccess) {
-            cudaGetLastError();
-            r->mem = nullptr;
-            settle();
-            return DG_E_OOM;
+        if (!r->mem) {  // not from the pool: allocate and clear the keys
+            if (r->fail_alloc || cudaMallocAsync(&r->mem, r->bytes, st) != cudaSuccess) {
+                cudaGetLastError();
+                r->mem = nullptr;
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->used -= r->bytes;
+                r->state = kDone;
+                r->status = DG_E_OOM;
+                r->t_done = now_s();
+                s->latencies_ms.push_back((r->t_done - r->t_submit) * 1e3);
+                s->cv_done.notify_all();
+                continue;
+            }
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->allocations++;
+            }
+            if (cudaMemsetAsync(r->mem, 0xFF, n * 8, st) != cudaSuccess) {
+                cudaGetLastError();
+                settle();
+                return DG_E_CUDA;
+            }
         }
         uint8_t* base = static_cast<uint8_t*>(r->mem);
         r->tgt.vis = reinterpret_cast<uint64_t*>(base);
@@ -145,10 +200,15 @@ dg_status launch_batch(dg_server* s, Slot* sl, std::vector<Request*>& batch, uin
         r->tgt.w = r->scene.width;
         r->tgt.h = r->scene.height;
         r->tgt.off_x = r->tgt.off_y = 0.0f;
-        if (cudaMemsetAsync(r->tgt.vis, 0xFF, n * 8, st) != cudaSuccess) {
-            settle();
-            return DG_E_CUDA;
-        }
+        run.push_back(r);
+    }
+    batch.swap(run);
+    if (batch.empty()) {
+        settle();
+        std::lock_guard<std::mutex> lk(s->mu);
+        sl->busy = false;
+        s->cv_sched.notify_all();
+        return DG_OK;
     }
     std::vector<Scene*> sc(batch.size());
     std::vector<FrameTarget> tg(batch.size());
@@ -166,11 +226,17 @@ dg_status launch_batch(dg_server* s, Slot* sl, std::vector<Request*>& batch, uin
     return DG_OK;
 }
 
+// The lane a request waits in (lane 0 when the server has no large-lane slot).
+int lane_of(const dg_server* s, uint64_t pixels, uint64_t tris) {
+    const bool large = pixels >= kLargePixels || tris >= kLargeTris;
+    return (large && s->slots.size() > 1) ? 1 : 0;
+}
+
 void scheduler(dg_server* s) {
     cudaSetDevice(s->ctx->device);
     std::unique_lock<std::mutex> lk(s->mu);
     for (;;) {
-        // release the buffers of finished discard requests
+        // release the buffers handed to the device
         if (!s->to_free.empty()) {
             std::vector<void*> fr;
             fr.swap(s->to_free);
@@ -182,84 +248,115 @@ void scheduler(dg_server* s) {
             lk.lock();
             s->used -= b;
         }
-        Slot* free_slot = nullptr;
         bool any_busy = false;
-        for (auto& sl : s->slots) {
-            if (sl->busy)
-                any_busy = true;
-            else if (!free_slot)
-                free_slot = sl.get();
-        }
-        if (s->stop && s->pending.empty() && !any_busy) break;
-        std::vector<Request*> batch;
-        uint64_t reserved = 0;  // growth of the slot's scratch this batch will cause
-        if (free_slot && !s->pending.empty()) {
+        for (auto& sl : s->slots) any_busy = any_busy || sl->busy;
+        const bool any_pending = !s->pending[0].empty() || !s->pending[1].empty();
+        if (s->stop && !any_pending && !any_busy) break;
+        bool launched = false, freed = false;
+        for (int lane = 0; lane < kLanes && !launched && !freed; lane++) {
+            std::deque<Request*>& q = s->pending[lane];
+            if (q.empty()) continue;
+            Slot* free_slot = nullptr;
+            for (auto& sl : s->slots)
+                if (!sl->busy && sl->lane == lane) {
+                    free_slot = sl.get();
+                    break;
+                }
+            if (!free_slot) continue;
             // admit in arrival order while the batch size and the memory budget allow; the
             // budget covers the requests' buffers and the scratch growth of the batch
+            std::vector<Request*> batch;
+            uint64_t reserved = 0;  // growth of the slot's scratch this batch will cause
             uint64_t V = 0, T = 0, P = 0;
             uint32_t L = 1;
             const uint64_t cur = free_slot->js.scratch_bytes;
-            while (!s->pending.empty() && batch.size() < s->max_batch) {
-                Request* r = s->pending.front();
+            const uint32_t cap = lane == 1 ? std::min(s->max_batch, kLargeBatch) : s->max_batch;
+            while (!q.empty() && batch.size() < cap) {
+                Request* r = q.front();
                 const Object& o = s->ctx->objects[r->scene.objects[0]];
                 const uint64_t V2 = V + o.nv, T2 = T + o.ntri_opaque, P2 = P + r->scene.width * r->scene.height;
                 const uint32_t L2 = std::max<uint32_t>(L, (uint32_t)r->scene.lights.size());
                 const uint64_t after = slot_scratch_after(free_slot->js, V2, T2, L2, P2);
                 const uint64_t grow_by = after > cur ? after - cur : 0;
-                if (s->used + r->bytes + (grow_by - reserved) > s->budget) break;
-                s->used += r->bytes + (grow_by - reserved);
+                auto pit = s->pool.find(r->size_key);
+                const bool pooled = !r->fail_alloc && pit != s->pool.end() && !pit->second.empty();
+                const uint64_t need = (grow_by - reserved) + (pooled ? 0 : r->bytes);
+                if (s->used + need > s->budget) {
+                    // release pooled buffers of other sizes, then try again
+                    for (auto& kv : s->pool) {
+                        if (kv.first == r->size_key) continue;
+                        const uint64_t w = kv.first >> 32, h = kv.first & 0xFFFFFFFFull;
+                        for (void* m : kv.second) {
+                            s->to_free.push_back(m);
+                            s->to_free_bytes.push_back(request_bytes(w, h));
+                            s->pooled_bytes -= request_bytes(w, h);
+                            freed = true;
+                        }
+                        kv.second.clear();
+                    }
+                    break;
+                }
+                if (pooled) {
+                    r->mem = pit->second.back();
+                    pit->second.pop_back();
+                    s->pooled_bytes -= r->bytes;
+                }
+                s->used += need;
                 reserved = grow_by;
                 V = V2;
                 T = T2;
                 P = P2;
                 L = L2;
                 s->peak_used = std::max(s->peak_used, s->used);
-                s->pending.pop_front();
+                q.pop_front();
                 r->state = kRunning;
                 r->t_start = now_s();
                 batch.push_back(r);
             }
-        }
-        if (batch.empty()) {
-            if (free_slot && !any_busy && !s->pending.empty() && s->held_done == 0 && s->to_free.empty()) {
-                // nothing runs and nothing waits to be collected, yet the head request
-                // (with the scratch its job needs) does not fit the budget: refuse it
-                Request* r = s->pending.front();
-                s->pending.pop_front();
-                r->state = kDone;
-                r->status = DG_E_OOM;
-                r->t_done = now_s();
-                s->cv_done.notify_all();
+            if (batch.empty()) {
+                if (!freed && !any_busy && s->held_done == 0 && s->to_free.empty()) {
+                    // nothing runs, nothing waits to be collected and no pooled buffer
+                    // can be released, yet the head request (with the scratch its job
+                    // needs) does not fit the budget: refuse it
+                    Request* r = q.front();
+                    q.pop_front();
+                    r->state = kDone;
+                    r->status = DG_E_OOM;
+                    r->t_done = now_s();
+                    s->cv_done.notify_all();
+                    freed = true;  // look at the queues again
+                }
                 continue;
             }
-            s->cv_sched.wait(lk);
-            continue;
-        }
-        free_slot->busy = true;
-        s->batches++;
-        lk.unlock();
-        dg_status e = launch_batch(s, free_slot, batch, reserved);
-        lk.lock();
-        if (e) {
-            // the batch did not launch: its requests complete with the error
-            if (!s->sticky) s->sticky = e;
-            const double t = now_s();
-            for (Request* r : batch) {
-                r->state = kDone;
-                r->status = e;
-                r->t_done = t;
-                if (r->mem) {
-                    s->to_free.push_back(r->mem);
-                    s->to_free_bytes.push_back(r->bytes);
-                    r->mem = nullptr;
-                } else {
-                    s->used -= r->bytes;
+            free_slot->busy = true;
+            s->batches++;
+            lk.unlock();
+            dg_status e = launch_batch(s, free_slot, batch, reserved);
+            lk.lock();
+            launched = true;
+            if (e) {
+                // the batch did not launch: its requests complete with the error
+                if (!s->sticky) s->sticky = e;
+                const double t = now_s();
+                for (Request* r : batch) {
+                    if (r->state == kDone) continue;
+                    r->state = kDone;
+                    r->status = e;
+                    r->t_done = t;
+                    if (r->mem) {
+                        s->to_free.push_back(r->mem);
+                        s->to_free_bytes.push_back(r->bytes);
+                        r->mem = nullptr;
+                    } else {
+                        s->used -= r->bytes;
+                    }
                 }
+                free_slot->batch.clear();
+                free_slot->busy = false;
+                s->cv_done.notify_all();
             }
-            free_slot->batch.clear();
-            free_slot->busy = false;
-            s->cv_done.notify_all();
         }
+        if (!launched && !freed) s->cv_sched.wait(lk);
     }
 }
 
@@ -297,6 +394,8 @@ dg_status dg_server_create(dg_ctx* ctx, uint64_t budget_bytes, uint32_t max_batc
         if (e) return e;
         if (cudaMallocHost((void**)&sl->h_err, 4) != cudaSuccess) return DG_E_OOM;
         *sl->h_err = 0;
+        // one slot in three (at least one) serves the large lane when there are two or more
+        sl->lane = (streams > 1 && i < std::max<uint32_t>(1u, streams / 3u)) ? 1 : 0;
         s->slots.push_back(std::move(sl));
     }
     s->thr = std::thread(scheduler, s.get());
@@ -323,14 +422,16 @@ dg_status dg_server_submit(dg_server* s, const dg_request* q, uint64_t* ticket) 
     if (e) return e;
     r->tgt.clear_depth = q->clear_depth;
     r->bytes = request_bytes(q->width, q->height);
+    r->size_key = ((uint64_t)q->width << 32) | q->height;
     r->discard = q->discard != 0;
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return DG_E_INVALID;
     if (r->bytes > s->budget) return DG_E_OOM;  // could never be admitted
+    r->lane = lane_of(s, (uint64_t)q->width * q->height, c->objects[q->object].ntri_opaque);
     r->ticket = s->next_ticket++;
     r->t_submit = now_s();
     *ticket = r->ticket;
-    s->pending.push_back(r.get());
+    s->pending[r->lane].push_back(r.get());
     s->reqs.emplace(r->ticket, std::move(r));
     s->cv_sched.notify_all();
     return DG_OK;
@@ -348,6 +449,7 @@ dg_status dg_server_wait(dg_server* s, uint64_t ticket, uint8_t* bgra, float* de
     if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
     void* mem = r->mem;
     const uint64_t bytes = r->bytes;
+    const uint64_t size_key = r->size_key;
     const uint64_t n = r->scene.width * r->scene.height;
     r->mem = nullptr;
     s->reqs.erase(it);
@@ -355,13 +457,19 @@ dg_status dg_server_wait(dg_server* s, uint64_t ticket, uint8_t* bgra, float* de
     if (mem) {
         cudaSetDevice(s->ctx->device);
         uint8_t* base = static_cast<uint8_t*>(mem);
+        const dg_status frame_st = st;
         if (st == DG_OK && bgra && cudaMemcpy(bgra, base + n * 8, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = DG_E_CUDA;
         if (st == DG_OK && depth && cudaMemcpy(depth, base + n * 12, n * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             st = DG_E_CUDA;
         lk.lock();
-        s->to_free.push_back(mem);
-        s->to_free_bytes.push_back(bytes);
+        if (frame_st == DG_OK) {  // the frame reset its keys: the buffers go back to the pool
+            s->pool[size_key].push_back(mem);
+            s->pooled_bytes += bytes;
+        } else {
+            s->to_free.push_back(mem);
+            s->to_free_bytes.push_back(bytes);
+        }
         s->held_done -= bytes;
         s->cv_sched.notify_all();
     }
@@ -378,10 +486,10 @@ dg_status dg_server_stats(dg_server* s, double* out, int32_t n) {
         size_t i = (size_t)std::min<double>(l.size() - 1, std::max(0.0, p * (l.size() - 1) + 0.5));
         return l[i];
     };
-    double v[8] = {(double)l.size(), pct(0.5), pct(0.99), l.empty() ? 0.0 : l.back(), (double)s->batches,
+    double v[9] = {(double)l.size(), pct(0.5), pct(0.99), l.empty() ? 0.0 : l.back(), (double)s->batches,
                    s->batches ? (double)s->frames / (double)s->batches : 0.0, (double)s->peak_used,
-                   (double)s->sticky};
-    for (int i = 0; i < n && i < 8; i++) out[i] = v[i];
+                   (double)s->sticky, (double)s->allocations};
+    for (int i = 0; i < n && i < 9; i++) out[i] = v[i];
     return DG_OK;
 }
 
@@ -391,7 +499,32 @@ dg_status dg_server_reset_stats(dg_server* s) {
     s->latencies_ms.clear();
     s->batches = 0;
     s->frames = 0;
+    s->allocations = 0;
     s->peak_used = s->used;
+    return DG_OK;
+}
+
+dg_status dg_server_cancel(dg_server* s, uint64_t ticket) {
+    if (!s) return DG_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end() || it->second->state != kPending) return DG_E_INVALID;
+    Request* r = it->second.get();
+    std::deque<Request*>& q = s->pending[r->lane];
+    q.erase(std::find(q.begin(), q.end(), r));
+    r->state = kDone;
+    r->status = DG_E_CANCELLED;
+    r->t_done = now_s();
+    s->cv_done.notify_all();
+    return DG_OK;
+}
+
+dg_status dg_server_inject_alloc_failure(dg_server* s, uint64_t ticket) {
+    if (!s) return DG_E_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end() || it->second->state != kPending) return DG_E_INVALID;
+    it->second->fail_alloc = true;
     return DG_OK;
 }
 
@@ -407,6 +540,8 @@ dg_status dg_server_destroy(dg_server* s) {
     for (auto& kv : s->reqs)
         if (kv.second->mem) cudaFreeAsync(kv.second->mem, s->copy_stream);
     for (void* p : s->to_free) cudaFreeAsync(p, s->copy_stream);
+    for (auto& kv : s->pool)
+        for (void* p : kv.second) cudaFreeAsync(p, s->copy_stream);
     cudaStreamSynchronize(s->copy_stream);
     for (auto& sl : s->slots) {
         cudaStream_t st = sl->js.stream;

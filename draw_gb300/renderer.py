@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libdrawgpu.so")
 DG_OK = 0
 STATUS = {
     1: "DG_E_INVALID", 2: "DG_E_INDEX", 3: "DG_E_TEXTURE_RANGE", 4: "DG_E_CAMERA", 5: "DG_E_DEPTH_UNINIT",
-    6: "DG_E_CUDA", 7: "DG_E_OOM", 8: "DG_E_LIMIT", 9: "DG_E_TIMEOUT",
+    6: "DG_E_CUDA", 7: "DG_E_OOM", 8: "DG_E_LIMIT", 9: "DG_E_TIMEOUT", 10: "DG_E_CANCELLED",
 }
 
 # Every symbol declared in include/draw_gpu.h, with its ctypes signature.
@@ -89,6 +89,8 @@ SIGNATURES = {
     "dg_server_wait": (_i32, [_P, _u64, _P, _P, _P]),
     "dg_server_stats": (_i32, [_P, _P, _i32]),
     "dg_server_reset_stats": (_i32, [_P]),
+    "dg_server_cancel": (_i32, [_P, _u64]),
+    "dg_server_inject_alloc_failure": (_i32, [_P, _u64]),
     "dg_server_destroy": (_i32, [_P]),
 }
 
@@ -147,13 +149,16 @@ _lib = None
 
 
 def load_library() -> ctypes.CDLL:
-    """Loads the in-tree libdrawgpu.so; raises if it has not been built."""
+    """Loads the in-tree libdrawgpu.so (or the in-tree library that
+    DRAW_GB300_LIB names, e.g. the DRAW_CHECKED build); raises if it has not
+    been built."""
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH):
-        raise RuntimeError(f"{LIB_PATH} is missing: build it with draw_gb300._build.build()")
-    lib = ctypes.CDLL(LIB_PATH)
+    path = os.environ.get("DRAW_GB300_LIB") or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with draw_gb300._build.build()")
+    lib = ctypes.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = res
@@ -746,10 +751,19 @@ class Server:
         return bgra, depth, lat.value
 
     def stats(self) -> dict:
-        v = (ctypes.c_double * 8)()
-        _chk(self.ctx.lib.dg_server_stats(self.h, v, 8), "server stats")
-        keys = ["completed", "p50_ms", "p99_ms", "max_ms", "batches", "mean_batch", "peak_bytes", "error"]
+        v = (ctypes.c_double * 9)()
+        _chk(self.ctx.lib.dg_server_stats(self.h, v, 9), "server stats")
+        keys = ["completed", "p50_ms", "p99_ms", "max_ms", "batches", "mean_batch", "peak_bytes", "error",
+                "allocations"]
         return dict(zip(keys, list(v)))
+
+    def cancel(self, ticket: int):
+        """dg_server_cancel: a request not admitted yet completes with DG_E_CANCELLED."""
+        _chk(self.ctx.lib.dg_server_cancel(self.h, ticket), "server cancel")
+
+    def inject_alloc_failure(self, ticket: int):
+        """dg_server_inject_alloc_failure (test hook): the request's buffer allocation fails."""
+        _chk(self.ctx.lib.dg_server_inject_alloc_failure(self.h, ticket), "server inject")
 
     def reset_stats(self):
         _chk(self.ctx.lib.dg_server_reset_stats(self.h), "server reset_stats")

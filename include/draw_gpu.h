@@ -38,6 +38,7 @@ typedef int32_t dg_status;
 #define DG_E_OOM 7            /* device memory exhausted or over budget */
 #define DG_E_LIMIT 8          /* size beyond a documented limit */
 #define DG_E_TIMEOUT 9        /* a bounded wait gave up */
+#define DG_E_CANCELLED 10     /* a render-server request cancelled before it was admitted */
 
 #define DG_MAX_LIGHTS 8
 
@@ -307,11 +308,16 @@ dg_status dg_autotune(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvase
  * resident (objects of the context), admits requests in arrival order against
  * a device-memory budget (each request holds W*H*16 bytes of colour, depth and
  * visibility buffers and 4 bytes per 32x32 pixel cell; job scratch counts too),
- * packs up to max_batch admitted
- * requests into one batched render job, and keeps up to `streams` jobs in flight
- * on separate streams. Each request renders exactly as dg_scene_render would
- * render it alone. While a server runs, its context must not be modified or
- * used for other rendering. */
+ * packs up to max_batch admitted requests into one batched render job, and
+ * keeps up to `streams` jobs in flight on separate streams. With two or more
+ * streams, requests of at least 1920x1080 pixels or 1M triangles wait in a
+ * lane of their own, served by one stream in three (at least one) in batches
+ * of at most 4, so smaller requests never queue behind them. Request buffers
+ * are pooled per frame size and reused without a clear; pooled buffers count
+ * against the budget and are released when a request of another size needs
+ * the room. Each request renders exactly as dg_scene_render would render it
+ * alone. While a server runs, its context must not be modified or used for
+ * other rendering. */
 typedef struct dg_server dg_server;
 
 typedef struct {
@@ -336,8 +342,18 @@ dg_status dg_server_submit(dg_server* s, const dg_request* r, uint64_t* ticket);
  * returns its status. latency_ms = completion - submission. */
 dg_status dg_server_wait(dg_server* s, uint64_t ticket, uint8_t* bgra, float* depth, double* latency_ms);
 /* [0] completed requests, [1] p50 latency ms, [2] p99 ms, [3] max ms, [4] batches,
- * [5] mean requests per batch, [6] peak device bytes held, [7] first launch error. */
+ * [5] mean requests per batch, [6] peak device bytes held, [7] first launch error,
+ * [8] request buffer sets allocated (the others were reused from the pool). */
 dg_status dg_server_stats(dg_server* s, double* out, int32_t n);
+/* Cancels a request that has not been admitted yet: it completes with
+ * DG_E_CANCELLED (collect it with dg_server_wait). DG_E_INVALID when the ticket
+ * is unknown or the request already runs or is done. */
+dg_status dg_server_cancel(dg_server* s, uint64_t ticket);
+/* Host-side fault injection for tests: the buffer allocation of this pending
+ * request is made to fail as if the device were out of memory, so it completes
+ * with DG_E_OOM while the rest of its batch renders. No GPU fault is involved.
+ * DG_E_INVALID when the ticket is unknown or no longer pending. */
+dg_status dg_server_inject_alloc_failure(dg_server* s, uint64_t ticket);
 dg_status dg_server_reset_stats(dg_server* s);
 /* Drains the pending requests, then frees the server. */
 dg_status dg_server_destroy(dg_server* s);

@@ -173,3 +173,61 @@ def test_server_admission_respects_budget(gpu_ctx):
     assert frame_bytes * 40 > budget  # the requests did not fit at once
     srv.close()
     ctx.close()
+
+
+def test_server_failures_injected_on_the_host(gpu_ctx):
+    """Host-side fault injection (no GPU fault): a request whose buffer
+    allocation is made to fail completes with DG_E_OOM while the requests
+    around it render; a pending request cancelled before admission completes
+    with DG_E_CANCELLED; malformed requests are refused at submission; and
+    buffers of finished requests are reused from the pool (fewer allocations
+    than requests)."""
+    from draw_gb300 import renderer as R
+
+    objs, texs, reqs = _pool()
+    ref = _alone(objs, texs, reqs[:8])
+    ctx = R.Context(0)
+    tm = [R.TextureMap(t.img, t.width, t.height, t.comps, ctx) for t in texs]
+    obs = [R.upload_object(o, tm, ctx) for o in objs]
+    srv = R.Server(ctx, budget_bytes=1 << 30, max_batch=4, streams=1)
+
+    def request(k, **kw):
+        oi, w, h, cam, light, e, clear = reqs[k]
+        return R.Server.request(obs[oi], w, h, cam, tuple(-c for c in cam), -0.5, -100.0, 60.0, light, e, clear,
+                                **kw)
+
+    # malformed requests
+    for bad in (dict(width=0), dict(height=70000), dict(nlights=0), dict(object=99)):
+        q = request(0)
+        for k, v in bad.items():
+            setattr(q, k, v)
+        with pytest.raises(R.DrawError) as e:
+            srv.submit(q)
+        assert e.value.status == 1, bad
+    # a burst of requests: the scheduler admits them in batches of 4 on one stream, so
+    # the later ones are still pending when the injections and the cancel arrive
+    blocker = [srv.submit(request(k % 8, discard=True)) for k in range(64)]
+    tickets = [srv.submit(request(k)) for k in range(8)]
+    srv.inject_alloc_failure(tickets[3])
+    srv.cancel(tickets[5])
+    with pytest.raises(R.DrawError):
+        srv.cancel(10 ** 9)  # unknown ticket
+    for t in blocker:
+        srv.wait(t)
+    for k, t in enumerate(tickets):
+        oi, w, h, *_r = reqs[k]
+        if k in (3, 5):
+            with pytest.raises(R.DrawError) as e:
+                srv.wait(t, w, h, read=True)
+            assert e.value.status == (7 if k == 3 else 10)
+            continue
+        bgra, depth, _lat = srv.wait(t, w, h, read=True)
+        p = compare(ref[k], (bgra, depth), reqs[k][6])
+        assert p.ok, f"request {k}: {describe(p)}"
+    with pytest.raises(R.DrawError):
+        srv.cancel(tickets[0])  # done already
+    st = srv.stats()
+    assert st["error"] == 0
+    assert st["allocations"] < len(blocker) + len(tickets) - 2  # buffers came back from the pool
+    srv.close()
+    ctx.close()
