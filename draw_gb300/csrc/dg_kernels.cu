@@ -661,67 +661,22 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
                 pending -= 32u;
             }
         };
-        // Exact stepping (fast edge sets whose box is small enough): when every
-        // term of every edge value over the box, |A| x + |B| y + |C| + |D| with
-        // the step of a unit included, stays below 2^24, all of them are integers
-        // that f32 holds exactly, so the reference's per-pixel expression equals
-        // the exact linear function, and a lane advances its three values by the
-        // exact change of one unit (A r32 + B q32, or with the carry into the next
-        // row A (r32 - w) + B (q32 + 1)) instead of evaluating them again. The
-        // coverage test on integer values is a comparison with -1/2 (tie edge:
-        // n >= 0) or 1/2 (n > 0).
-        bool exact = fast;
-        if (fast) {
-            const float X = (float)(xlo + w), Y = (float)(ylo + (npx + w - 1u) / w + DG_UNIT_PX + 1u);
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                const float S = fA(fA(fA(fM(fabsf(e.A[j]), X), fM(fabsf(e.B[j]), Y)), fabsf(e.C[j])), fabsf(e.D[j]));
-                exact = exact && S < 16000000.0f;
+        for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
+            bool cand = false;
+            const uint32_t x = xlo + xx, y = ylo + yy;
+            xx += r32;
+            yy += q32;
+            if (xx >= w) {
+                xx -= w;
+                yy++;
             }
-        }
-        if (exact) {
-            const float x0 = (float)(xlo + xx), y0 = (float)(ylo + yy);
-            float n0 = edge_eval(e, 0, x0, y0), n1 = edge_eval(e, 1, x0, y0), n2 = edge_eval(e, 2, x0, y0);
-            const float fr32 = (float)r32, fq32 = (float)q32;
-            const float frc = -(float)(w - r32), fqc = (float)(q32 + 1u);
-            const float dq0 = fA(fM(e.A[0], fr32), fM(e.B[0], fq32)), dc0 = fA(fM(e.A[0], frc), fM(e.B[0], fqc));
-            const float dq1 = fA(fM(e.A[1], fr32), fM(e.B[1], fq32)), dc1 = fA(fM(e.A[1], frc), fM(e.B[1], fqc));
-            const float dq2 = fA(fM(e.A[2], fr32), fM(e.B[2], fq32)), dc2 = fA(fM(e.A[2], frc), fM(e.B[2], fqc));
-            const float th0 = (e.tie & 1u) ? -0.5f : 0.5f, th1 = (e.tie & 2u) ? -0.5f : 0.5f,
-                        th2 = (e.tie & 4u) ? -0.5f : 0.5f;
-            for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
-                const uint32_t x = xlo + xx, y = ylo + yy;
-                const bool cand = k < npx && n0 > th0 && n1 > th1 && n2 > th2;
-                xx += r32;
-                yy += q32;
-                const bool carry = xx >= w;
-                if (carry) {
-                    xx -= w;
-                    yy++;
-                }
-                n0 = fA(n0, carry ? dc0 : dq0);
-                n1 = fA(n1, carry ? dc1 : dq1);
-                n2 = fA(n2, carry ? dc2 : dq2);
-                push(cand, x, y);
+            if (k < npx) {
+                const float xf = (float)x, yf = (float)y;
+                const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
+                cand = fast ? covered_signs(e.tie, n0, n1, n2)
+                            : !(prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2]));
             }
-        } else {
-            for (uint32_t u = item.y; u < u_end; u++, k += DG_UNIT_PX) {
-                bool cand = false;
-                const uint32_t x = xlo + xx, y = ylo + yy;
-                xx += r32;
-                yy += q32;
-                if (xx >= w) {
-                    xx -= w;
-                    yy++;
-                }
-                if (k < npx) {
-                    const float xf = (float)x, yf = (float)y;
-                    const float n0 = edge_eval(e, 0, xf, yf), n1 = edge_eval(e, 1, xf, yf), n2 = edge_eval(e, 2, xf, yf);
-                    cand = fast ? covered_signs(e.tie, n0, n1, n2)
-                                : !(prereject(n0, e.den[0]) || prereject(n1, e.den[1]) || prereject(n2, e.den[2]));
-                }
-                push(cand, x, y);
-            }
+            push(cand, x, y);
         }
         __syncwarp();
         if (lane < pending) finish_fragment(R, seq, bx[lane], by[lane], clear_depth, vis, width, rcp, yr);

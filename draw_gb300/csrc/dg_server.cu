@@ -4,7 +4,8 @@
 // lights) from any thread. Requests go to one of two lanes: large ones (at
 // least 1920x1080 pixels or 1M triangles) and the rest, each lane with its own
 // arrival-ordered queue and its own job slots (stream and scratch), so a small
-// request never waits behind a large frame. A scheduler thread admits pending
+// request never waits behind a large frame; a slot whose own lane is empty
+// takes requests of the other lane. A scheduler thread admits pending
 // requests of a lane in arrival order while the device-memory budget allows
 // (each request holds colour, depth and visibility buffers; job-slot scratch
 // counts too), packs up to max_batch of them (large lane: at most
@@ -46,7 +47,7 @@ double now_s() {
 enum ReqState { kPending = 0, kRunning = 1, kDone = 2 };
 
 constexpr int kLanes = 2;            // 0: small requests, 1: large ones
-constexpr uint32_t kLargeBatch = 4;  // requests per batch in the large lane
+constexpr uint32_t kLargeBatch = 16;  // requests per batch in the large lane
 constexpr uint64_t kLargePixels = 1920ull * 1080ull;
 constexpr uint64_t kLargeTris = 1000000ull;
 
@@ -253,12 +254,17 @@ void scheduler(dg_server* s) {
         const bool any_pending = !s->pending[0].empty() || !s->pending[1].empty();
         if (s->stop && !any_pending && !any_busy) break;
         bool launched = false, freed = false;
-        for (int lane = 0; lane < kLanes && !launched && !freed; lane++) {
+        for (int pass = 0; pass < 2 * kLanes && !launched && !freed; pass++) {
+            // passes 0, 1: each lane's queue on a free slot of that lane; passes 2, 3:
+            // a lane's queue on a free slot of the other lane (whose own queue is empty)
+            const int lane = pass % kLanes;
+            const int slot_lane = pass < kLanes ? lane : 1 - lane;
             std::deque<Request*>& q = s->pending[lane];
             if (q.empty()) continue;
+            if (pass >= kLanes && !s->pending[slot_lane].empty()) continue;
             Slot* free_slot = nullptr;
             for (auto& sl : s->slots)
-                if (!sl->busy && sl->lane == lane) {
+                if (!sl->busy && sl->lane == slot_lane) {
                     free_slot = sl.get();
                     break;
                 }

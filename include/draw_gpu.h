@@ -312,7 +312,8 @@ dg_status dg_autotune(dg_ctx* ctx, const int32_t* scenes, const int32_t* canvase
  * keeps up to `streams` jobs in flight on separate streams. With two or more
  * streams, requests of at least 1920x1080 pixels or 1M triangles wait in a
  * lane of their own, served by one stream in three (at least one) in batches
- * of at most 4, so smaller requests never queue behind them. Request buffers
+ * of at most 16, so smaller requests never queue behind them (a stream whose
+ * lane has nothing pending takes the other lane's requests). Request buffers
  * are pooled per frame size and reused without a clear; pooled buffers count
  * against the budget and are released when a request of another size needs
  * the room. Each request renders exactly as dg_scene_render would render it
