@@ -498,7 +498,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     uint64_t total_vtx = 0, total_tri = 0, total_tiles = 0, total_px = 0;
     uint64_t ntt = 0, tmesh_total = 0, max_frame_tt = 0;
     uint32_t stride = 1;
-    bool any_persp = false;
+    bool any_persp = false, any_lazy = false;
     B.transparent_objects.clear();
     for (uint32_t i = 0; i < n; i++) {
         Scene& s = *scenes[i];  // frame_setup updates the camera basis, as Scene::render does
@@ -532,6 +532,23 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         f.exponent = s.exponent;
         f.flags = s.interpolation == DG_INTERP_PERSPECTIVE ? DG_FRAME_PERSPECTIVE : 0u;
         any_persp = any_persp || f.flags != 0u;
+        {
+            // At least as many opaque triangles as pixels, and a light/halfway table
+            // (32 bytes per vertex and light) beyond the L2: the small triangles'
+            // vertices get no rows, and their shading computes the vectors for the
+            // pixels they win. Measured: the 3840x2160 frame of 10M micro triangles and
+            // 4 lights gains 5% (most of its triangles win no pixel); a 256x256 frame of
+            // a 300k-triangle mesh and 1 light (a 5 MB table) lost 14%, so it keeps rows.
+            uint64_t frame_tris = 0, frame_vtx = 0;
+            for (int32_t oid : s.objects) {
+                frame_tris += c->objects[oid].ntri_opaque;
+                frame_vtx += c->objects[oid].nv;
+            }
+            if (frame_tris >= tg.w * tg.h && frame_vtx * s.lights.size() * 32u >= (128ull << 20)) {
+                f.flags |= DG_FRAME_LAZY;
+                any_lazy = true;
+            }
+        }
         f.off_x = tg.off_x;
         f.off_y = tg.off_y;
         f.width = (uint32_t)tg.w;
@@ -697,6 +714,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.trec = S.d_trec;
     job.trec_w = any_persp ? S.d_trec_w : nullptr;
     job.ext = any_persp ? 1u : 0u;
+    job.lazy = any_lazy ? 1u : 0u;
     for (const TexMap& t : c->tex)
         if (t.filter != DG_FILTER_NEAREST) job.ext = 1u;
     job.ttrec_w = any_persp && ntt ? S.d_ttrec_w : nullptr;

@@ -844,9 +844,20 @@ __device__ __forceinline__ const float4* shade_row(const DgJobDev& job, uint32_t
 
 // Shades the winning fragment of pixel (x, y) from its triangle record:
 // canvas.rs:682-741.
+// World position of job vertex v (the segment that holds it, then its position).
+__device__ __forceinline__ V3 job_vertex(const DgJobDev& job, uint32_t v) {
+    const uint32_t si = last_le(job.nsegs, v, [&](uint32_t i) { return job.segs[i].vtx_begin; });
+    const DgSegDev& sg = job.segs[si];
+    const float4 p4 = __ldg(sg.pos + (v - sg.vtx_begin));
+    return V3{p4.x, p4.y, p4.z};
+}
+
 // Wp (frames with DG_FRAME_PERSPECTIVE, else null): the record's inv_w3. EXT
 // as for shade_colour (false: the reference's interpolation and fetch only).
-template <bool EXT>
+// LAZY: the record may carry DG_TRI_LAZY, and then the light/halfway vectors of
+// its three vertices are computed here from their positions (shade_vertex's
+// operations) instead of read from job.vshade.
+template <bool EXT, bool LAZY>
 __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const DgFrameDev& fr, const DgTriRec* R,
                                                       uint32_t x, uint32_t y, const float* inv255,
                                                       const DgTexDev* stex, float& depth_out, int& errc,
@@ -875,19 +886,37 @@ __device__ __forceinline__ uint32_t shade_from_record(const DgJobDev& job, const
     m.ks = V3{__uint_as_float(rows.w), __uint_as_float(last.x), __uint_as_float(last.y)};
     m.map_ka = last.z;
     m.map_kd = last.w;
+    const bool lazy = LAZY && (e.tie & DG_TRI_LAZY) != 0u;
     auto lv = [&](uint32_t l, V3& lt, V3& h) {
-        if (DG_CHECKED) {
-            const uint32_t nrow = job.total_vtx + job.vrow_extra + 6u * job.ntt;
-            if (!DG_IN_RANGE(rows.x < nrow && rows.y < nrow && rows.z < nrow, job.err)) {
-                lt = h = V3{0.0f, 0.0f, 0.0f};
-                return;
+        float4 a, b, c, a1, b1, c1;
+        if (LAZY && lazy) {
+            // each vertex again per light (positions are cached loads): nothing is
+            // held across the lights, which keeps the registers of the common path
+            const V3 cam = {fr.cam[0], fr.cam[1], fr.cam[2]};
+            auto vtx = [&](uint32_t v, float4& o0, float4& o1) {
+                const V3 p = job_vertex(job, v);
+                V3 t, hh;
+                light_halfway(fr, p, vnormalized(vsub(p, cam)), l, t, hh);
+                o0 = make_float4(t.x, t.y, t.z, hh.x);
+                o1 = make_float4(hh.y, hh.z, 0.0f, 0.0f);
+            };
+            vtx(rows.x, a, a1);
+            vtx(rows.y, b, b1);
+            vtx(rows.z, c, c1);
+        } else {
+            if (DG_CHECKED) {
+                const uint32_t nrow = job.total_vtx + job.vrow_extra + 6u * job.ntt;
+                if (!DG_IN_RANGE(rows.x < nrow && rows.y < nrow && rows.z < nrow, job.err)) {
+                    lt = h = V3{0.0f, 0.0f, 0.0f};
+                    return;
+                }
             }
+            const float4* pa = shade_row(job, rows.x, l);
+            const float4* pb = shade_row(job, rows.y, l);
+            const float4* pc = shade_row(job, rows.z, l);
+            a = __ldg(pa), b = __ldg(pb), c = __ldg(pc);
+            a1 = __ldg(pa + 1), b1 = __ldg(pb + 1), c1 = __ldg(pc + 1);
         }
-        const float4* pa = shade_row(job, rows.x, l);
-        const float4* pb = shade_row(job, rows.y, l);
-        const float4* pc = shade_row(job, rows.z, l);
-        const float4 a = __ldg(pa), b = __ldg(pb), c = __ldg(pc);
-        const float4 a1 = __ldg(pa + 1), b1 = __ldg(pb + 1), c1 = __ldg(pc + 1);
         lt = V3{interp(al, be, ga, a.x, b.x, c.x), interp(al, be, ga, a.y, b.y, c.y),
                 interp(al, be, ga, a.z, b.z, c.z)};
         h = V3{interp(al, be, ga, a.w, b.w, c.w), interp(al, be, ga, a1.x, b1.x, c1.x),

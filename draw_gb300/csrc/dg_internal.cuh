@@ -103,6 +103,11 @@ struct alignas(16) DgFrameDev {
     uint32_t pad;
 };
 #define DG_FRAME_PERSPECTIVE 1u
+// The frame has at least as many triangles as pixels: its small triangles
+// (boxes of at most small_max_px pixels) get no light/halfway rows; the
+// resolve pass computes their vertices' vectors for the pixels they win
+// (DG_TRI_LAZY in the record's tie word).
+#define DG_FRAME_LAZY 2u
 static_assert(sizeof(DgTexDev) == 48 && sizeof(DgMatDev) == 48, "descriptor sizes");
 inline uint32_t dg_tex_small(uint64_t len, uint64_t w, uint64_t h) {
     return (len < (1ull << 32) && w < (1ull << 24) && h < (1ull << 24)) ? 1u : 0u;
@@ -154,6 +159,10 @@ struct DgEdges {
 // Set in DgEdges.tie when every den is finite and > 0 (edges are stored
 // normalized to a den without sign bit): coverage is then a sign test.
 #define DG_EDGE_FAST 8u
+// Set in a triangle record's tie word when its vertices have no light/halfway
+// rows (DG_FRAME_LAZY): shading computes them from the vertex positions, with
+// the same functions that fill the rows, so the values are identical.
+#define DG_TRI_LAZY 16u
 
 // One triangle (or one clip output of it) as the raster and shade passes read
 // it: twelve 16-byte words. Attribute fields hold the three vertices' values
@@ -222,6 +231,7 @@ struct DgJobDev {
     float4* trec_w;
     float4* ttrec_w;
     uint32_t ext;  // 1: a frame uses perspective-correct interpolation or a texture map the bilinear filter
+    uint32_t lazy;  // 1: a frame has DG_FRAME_LAZY
     uint32_t trec_cap;
     uint32_t queue_cap;
     DgQueueRec* queue;

@@ -243,7 +243,9 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
                     clipped = true;
                     if (nout > 0 && P.nv > 3) nrows = (uint32_t)(P.nv - 3);  // light rows for the new vertices
                 }
-                if (nout > 0) {  // its vertices need light/halfway vectors for shading
+                // its vertices need light/halfway vectors for shading (in a DG_FRAME_LAZY
+                // frame an unclipped triangle is marked below, unless its record is lazy)
+                if (nout > 0 && (clipped || !(job.frames[sg.frame].flags & DG_FRAME_LAZY))) {
                     const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
                     for (int k = 0; k < 3; k++) job.vmark[vv[k]] = 1u;  // plain stores: every writer writes 1
                 }
@@ -311,6 +313,15 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
                         bbox_axis(tr.ay, tr.by, tr.cy, fr.height, tr.ylo, tr.yhi);
                         boxed = true;
                         make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
+                        const uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
+                        if ((fr.flags & DG_FRAME_LAZY) && !clipped) {
+                            if (rbase != DG_NONE && px <= job.small_max_px) {
+                                e.tie |= DG_TRI_LAZY;  // no rows: shading computes the vertices' vectors
+                            } else {
+                                const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
+                                for (int k = 0; k < 3; k++) job.vmark[vv[k]] = 1u;
+                            }
+                        }
                         if (rbase != DG_NONE) {
                             float4* wout = (fr.flags & DG_FRAME_PERSPECTIVE) && job.trec_w
                                                ? job.trec_w + rbase + (uint32_t)rr
@@ -321,7 +332,6 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
                                 write_clip_record(job, job.trec + rbase + (uint32_t)rr, sg, tp, tuv, tnr, e, tr, P, rr,
                                                   job.total_vtx + row0, fr, wout);
                         }
-                        uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
                         if (rbase == DG_NONE) {
                             inplace = true;
                         } else if (px <= job.small_max_px) {
@@ -753,7 +763,9 @@ __device__ __forceinline__ void resolve_prologue(const DgJobDev& job, float* inv
 // One tile of the resolve pass (block-uniform; the tables of resolve_prologue
 // must be in place). EXT: the job uses an extension mode (perspective-correct
 // interpolation or bilinear fetch); false compiles the reference's shading only.
-template <uint32_t TH, bool EXT>
+// LAZY: a frame of the job has DG_FRAME_LAZY (records of small triangles carry
+// no light rows).
+template <uint32_t TH, bool EXT, bool LAZY>
 __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint32_t tile, const float* inv255,
                                                  const DgTexDev* stex) {
     __shared__ uint16_t s_pix[DG_TILE_W * TH];  // pixel index within the tile
@@ -871,7 +883,7 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
         float d = 0.0f;
         int errc;
         const float4* wp = EXT && (fr.flags & DG_FRAME_PERSPECTIVE) && job.trec_w ? job.trec_w + s_val[k] : nullptr;
-        uint32_t c = shade_from_record<EXT>(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc, wp);
+        uint32_t c = shade_from_record<EXT, LAZY>(job, fr, job.trec + s_val[k], px, py, inv255, stex, d, errc, wp);
         if (errc != DG_OK) c = AZUL_BB;
         // one error-word update per warp (every pixel of a bad job may fail)
         const unsigned act = __activemask();
@@ -884,13 +896,13 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
     if (any_no_record) shade_tile_without_records<TH>(job, tile, inv255, stex);
 }
 
-template <uint32_t TH, bool EXT>
+template <uint32_t TH, bool EXT, bool LAZY>
 __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
     __shared__ float inv255[256];
     __shared__ DgTexDev stex[DG_SMEM_TEX];
     resolve_prologue(job, inv255, stex);
     wait_previous_kernel();
-    dev_resolve_tile<TH, EXT>(job, blockIdx.x, inv255, stex);
+    dev_resolve_tile<TH, EXT, LAZY>(job, blockIdx.x, inv255, stex);
 }
 
 __global__ void k_fill(uint32_t* colour, float* depth, uint64_t n, uint32_t cv, float dv, int fc, int fd) {
@@ -961,10 +973,14 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
     if ((e = dg_launch_transparent(1, job, cfg.tplan, s)) != cudaSuccess) return e;
     if (job.total_tiles) {
         NvtxRange r("k_resolve");
-        auto kr = job.ext ? (job.tile_rows == 8u ? k_resolve<8, true> : job.tile_rows == 16u ? k_resolve<16, true>
-                                                                                         : k_resolve<32, true>)
-                          : (job.tile_rows == 8u ? k_resolve<8, false> : job.tile_rows == 16u ? k_resolve<16, false>
-                                                                                              : k_resolve<32, false>);
+        using KR = void (*)(const DgJobDev);
+        // [lazy][ext][tile rows 8, 16, 32]
+        static const KR kr_table[2][2][3] = {
+            {{k_resolve<8, false, false>, k_resolve<16, false, false>, k_resolve<32, false, false>},
+             {k_resolve<8, true, false>, k_resolve<16, true, false>, k_resolve<32, true, false>}},
+            {{k_resolve<8, false, true>, k_resolve<16, false, true>, k_resolve<32, false, true>},
+             {k_resolve<8, true, true>, k_resolve<16, true, true>, k_resolve<32, true, true>}}};
+        const KR kr = kr_table[job.lazy ? 1 : 0][job.ext ? 1 : 0][job.tile_rows == 8u ? 0 : job.tile_rows == 16u ? 1 : 2];
         if ((e = launch_dependent(kr, job.total_tiles, 256, job, s)) != cudaSuccess) return e;
     }
     // part 2: the ordered blend over the opaque colours

@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(256) k_tfold(const DgJobDev job) {
             float d;
             int errc;
             const float4* wp = (fr.flags & DG_FRAME_PERSPECTIVE) && job.ttrec_w ? job.ttrec_w + rec : nullptr;
-            uint32_t c = shade_from_record<true>(job, fr, job.ttrec + rec, x, y, inv255, stex, d, errc, wp);
+            uint32_t c = shade_from_record<true, false>(job, fr, job.ttrec + rec, x, y, inv255, stex, d, errc, wp);
             if (errc != DG_OK) bits |= 1u << errc;
             const float a = __ldcg(job.talpha + rec);
             if (a < 1.0f) c = px_add(px_mul(bg, fS(1.0f, a)), px_mul(c, a));

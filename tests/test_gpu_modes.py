@@ -115,3 +115,11 @@ def test_mode_arguments_validated(gpu_ctx):
         b.scene.set_interpolation(2)
     with pytest.raises(renderer.DrawError):
         b.texmaps[0].set_filter(-1)
+
+
+def test_modes_dense_frame(gpu_ctx, oracle_lib):
+    """Both extensions on a frame with more triangles than pixels (lazy vertex
+    shading of its small triangles)."""
+    from test_gpu_parity import _dense_torus
+
+    _check(_with_modes(_dense_torus(), 1, 1), gpu_ctx, 5000)

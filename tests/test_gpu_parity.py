@@ -209,3 +209,37 @@ def test_seeded_random_scenes_and_tunings(seed, gpu_ctx, oracle_lib):
         assert p.ok, f"{desc.name} {knobs}: {describe(p)}; {first_mismatch(ref, got)}"
     finally:
         gpu_ctx.set_tuning(**before)
+
+
+def _dense_torus(n_tris=2_200_000, w=200, h=150, lights=4):
+    """A frame with more triangles than pixels and a light/halfway table beyond
+    128 MB (1.1M vertices x 4 lights x 32 bytes), so DG_FRAME_LAZY: the records
+    of its small triangles carry no light rows and the resolve pass computes
+    their vertices' light/halfway vectors for the pixels they win."""
+    pos, nrm, uv, tri = S.mesh_for_tris("torus", n_tris)
+    mat = S.Material((0.1,) * 3, (0.7,) * 3, (0.2,) * 3, 1.0, 0, 0)
+    cam = (0.4, 1.4, 2.5)
+    return S.SceneDesc(w, h, cam_pos=cam, cam_dir=tuple(-c for c in cam), near=-0.5, far=-100.0, fov_x=60.0,
+                       lights=np.array([[3.0, 4.0, 3.0], [-2.0, 1.0, 4.0], [0.5, -3.0, 2.0], [-3.0, -2.0, 1.0]][:lights],
+                                       np.float32),
+                       exponent=5, textures=[S.value_noise_checker(256, 256, 21)],
+                       objects=[S.ObjectDesc(pos, nrm, uv, [S.MeshDesc(S._tris9(tri), 0)], [mat])],
+                       name=f"dense_torus{n_tris}@{w}x{h}")
+
+
+def test_parity_dense_frame_lazy_vertex_shading(gpu_ctx, oracle_lib):
+    desc = _dense_torus()
+    assert desc.n_tris >= desc.width * desc.height
+    assert desc.objects[0].vertices.shape[0] * len(desc.lights) * 32 >= 128 << 20
+    ref = oracle_render(desc)
+    got = gpu_render(desc, gpu_ctx)
+    p = compare(ref, got, desc.clear_depth)
+    assert p.ok and p.n_covered > 5000, f"{describe(p)}; {first_mismatch(ref, got)}"
+    # the same frame with the small-triangle path off (every triangle queued): records with rows
+    before = gpu_ctx.get_tuning()
+    try:
+        gpu_ctx.set_tuning(small_max_px=0)
+        got2 = gpu_render(desc, gpu_ctx)
+    finally:
+        gpu_ctx.set_tuning(**before)
+    assert np.array_equal(got[0], got2[0]) and np.array_equal(got[1].view(np.uint32), got2[1].view(np.uint32))
