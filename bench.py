@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-torus", action="store_true", help="skip the torus leg")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-batch", type=int, default=64, help="server: requests per batch")
+    ap.add_argument("--serve-streams", type=int, default=3, help="server: batches in flight")
     ap.add_argument("--batch-frames", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--kernel-steps", type=int, default=500,
@@ -440,7 +442,8 @@ def run_ours(args, world, rank, local):
         line["batched"] = batched_leg(ctx, stream, args.batch_frames)
 
     if rank == 0 and world == 1 and not args.no_serve:
-        line["served"] = serving_leg(local, seconds=args.serve_seconds, rate=args.serve_rate)
+        line["served"] = serving_leg(local, seconds=args.serve_seconds, rate=args.serve_rate,
+                                     max_batch=args.serve_batch, streams=args.serve_streams)
 
     if rank == 0 and world == 1 and not args.no_stress:
         line["stress"] = stress_leg(ctx, stream, flush, peak, cpu=not args.no_cpu)
@@ -688,7 +691,7 @@ SERVE_P = [0.4, 0.3, 0.2, 0.1]
 
 
 def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes: int = 64, n_tex: int = 32,
-                budget: int = 40 << 30, seed: int = 1234) -> dict:
+                budget: int = 40 << 30, seed: int = 1234, max_batch: int = 64, streams: int = 3) -> dict:
     """Serving workload: Poisson request stream against a resident pool of meshes
     and textures, served by the continuous-batching server (dg_server_*), next to
     the plain one-frame-per-launch path on the same request mix."""
@@ -772,7 +775,7 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
         plain_class_ms.setdefault(f"{w}x{h}", []).append(a.elapsed_time(b_))
     ctx.set_stream(None)
 
-    srv = R.Server(ctx, budget_bytes=budget, max_batch=64, streams=3)
+    srv = R.Server(ctx, budget_bytes=budget, max_batch=max_batch, streams=streams)
 
     def req(q):
         oi, w, h, cam, light = q
@@ -839,7 +842,8 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
     return {
         "workload": f"Poisson {rate:.0f} req/s for {seconds:.0f} s; resolution {SERVE_RES} with p={SERVE_P}; "
                     f"{n_meshes} resident meshes of 5k..2M triangles (log-uniform, {sum(ntris) / 1e6:.1f}M total), "
-                    f"{n_tex} resident 512^2 textures; budget {budget / 2**30:.0f} GiB; max batch 64, 3 streams",
+                    f"{n_tex} resident 512^2 textures; budget {budget / 2**30:.0f} GiB; max batch {max_batch}, "
+                    f"{streams} streams",
         "pool_build_s": gen_s,
         "plain_frames_per_s": len(plain_reqs) / plain_dev, "plain_wall_frames_per_s": len(plain_reqs) / plain_wall,
         "saturated_frames_per_s": len(sat_reqs) / sat_s, "saturated_mean_batch": sat_stats["mean_batch"],

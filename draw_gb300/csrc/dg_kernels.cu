@@ -694,8 +694,12 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
     }
 }
 
+// The resolve pass may start only after this kernel's blocks have waited for
+// the setup pass, so that its early clear of untouched tiles (k_resolve) reads
+// a complete cell map: the wait comes before the launch signal here.
 __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
-    wait_previous_kernel();
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    allow_next_kernel();
     dev_queue(job);
 }
 
@@ -760,6 +764,39 @@ __device__ __forceinline__ void resolve_prologue(const DgJobDev& job, float* inv
         reinterpret_cast<uint4*>(stex)[i] = __ldg(reinterpret_cast<const uint4*>(job.tex) + i);
 }
 
+// Canvas::clear (canvas.rs:425-433) of one 32 x TH tile (tile column tx, row ty):
+// 16-byte stores of four pixels where the rows are 16-byte aligned.
+template <uint32_t TH>
+__device__ __forceinline__ void clear_tile(const DgFrameDev& fr, uint32_t tx, uint32_t ty) {
+    const uint32_t W = fr.width, H = fr.height;
+    const uint32_t x0 = tx * DG_TILE_W;
+    const bool vec = (W & 3u) == 0u && x0 + DG_TILE_W <= W &&
+                     ((reinterpret_cast<uintptr_t>(fr.depth) | reinterpret_cast<uintptr_t>(fr.colour)) & 15u) == 0u;
+    if (vec) {
+        const uint32_t r = threadIdx.x >> 3, c = (threadIdx.x & 7u) * 4u;
+        const float cd = fr.clear_depth;
+        for (uint32_t yy = r; yy < TH; yy += 32u) {
+            const uint32_t y = ty * TH + yy;
+            if (y < H) {
+                *reinterpret_cast<float4*>(fr.depth + (uint64_t)y * W + x0 + c) = make_float4(cd, cd, cd, cd);
+                *reinterpret_cast<uint4*>(fr.colour + (uint64_t)(H - 1u - y) * W + x0 + c) =
+                    make_uint4(AZUL_BB, AZUL_BB, AZUL_BB, AZUL_BB);
+            }
+        }
+        return;
+    }
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint32_t x = x0 + lane;
+#pragma unroll
+    for (uint32_t j = 0; j < TH / 8u; j++) {
+        const uint32_t y = ty * TH + wid + 8u * j;
+        if (x < W && y < H) {
+            fr.depth[(uint64_t)y * W + x] = fr.clear_depth;
+            fr.colour[(uint64_t)(H - 1u - y) * W + x] = AZUL_BB;
+        }
+    }
+}
+
 // One tile of the resolve pass (block-uniform; the tables of resolve_prologue
 // must be in place). EXT: the job uses an extension mode (perspective-correct
 // interpolation or bilinear fetch); false compiles the reference's shading only.
@@ -782,31 +819,7 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
     if (fr.cells != nullptr && __ldcg(fr.cells + ((ty * TH) >> 5) * fr.tiles_x + tx) != fr.epoch) {
         // No triangle's box reached the tile's 32x32 cell this frame, so all its
         // keys are empty: the clear values, without reading the keys (block-uniform).
-        // 16-byte stores of four pixels where the rows are 16-byte aligned.
-        const uint32_t x0 = tx * DG_TILE_W;
-        const bool vec = (W & 3u) == 0u && x0 + DG_TILE_W <= W &&
-                         ((reinterpret_cast<uintptr_t>(fr.depth) | reinterpret_cast<uintptr_t>(fr.colour)) & 15u) == 0u;
-        if (vec) {
-            const uint32_t r = threadIdx.x >> 3, c = (threadIdx.x & 7u) * 4u;
-            const float cd = fr.clear_depth;
-            for (uint32_t yy = r; yy < TH; yy += 32u) {
-                const uint32_t y = ty * TH + yy;
-                if (y < H) {
-                    *reinterpret_cast<float4*>(fr.depth + (uint64_t)y * W + x0 + c) = make_float4(cd, cd, cd, cd);
-                    *reinterpret_cast<uint4*>(fr.colour + (uint64_t)(H - 1u - y) * W + x0 + c) =
-                        make_uint4(AZUL_BB, AZUL_BB, AZUL_BB, AZUL_BB);
-                }
-            }
-            return;
-        }
-#pragma unroll
-        for (int j = 0; j < R; j++) {
-            const uint32_t y = ty * TH + wid + 8u * j;
-            if (x < W && y < H) {
-                fr.depth[(uint64_t)y * W + x] = fr.clear_depth;
-                fr.colour[(uint64_t)(H - 1u - y) * W + x] = AZUL_BB;
-            }
-        }
+        clear_tile<TH>(fr, tx, ty);
         return;
     }
     uint64_t key[R];
@@ -901,6 +914,22 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJo
     __shared__ float inv255[256];
     __shared__ DgTexDev stex[DG_SMEM_TEX];
     resolve_prologue(job, inv255, stex);
+    if (job.ntt == 0u) {
+        // A tile that no triangle box reached is cleared before waiting for the
+        // raster pass: its keys are all empty, and the cell map it reads is complete
+        // (k_queue_raster signals this kernel only after it waited for the setup
+        // pass). With a transparent pass, the kernel before this one is not the queue
+        // pass, and every tile waits.
+        const uint32_t tile = blockIdx.x;
+        const uint32_t fi = last_le(job.nframes, tile, [&](uint32_t i) { return job.frames[i].tile_begin; });
+        const DgFrameDev& fr = job.frames[fi];
+        const uint32_t lt = tile - fr.tile_begin;
+        const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
+        if (fr.cells != nullptr && __ldcg(fr.cells + ((ty * TH) >> 5) * fr.tiles_x + tx) != fr.epoch) {
+            clear_tile<TH>(fr, tx, ty);
+            return;
+        }
+    }
     wait_previous_kernel();
     dev_resolve_tile<TH, EXT, LAZY>(job, blockIdx.x, inv255, stex);
 }
