@@ -500,6 +500,27 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     uint32_t stride = 1;
     bool any_persp = false, any_lazy = false;
     B.transparent_objects.clear();
+    // Resolve tile height: the tile_rows knob, or (0) the tallest of 32, 16 and 8
+    // rows whose tiles fill the resolve pass's resident blocks (4 per SM), else 8.
+    // A tile's threads shade its covered pixels one after another (up to 4 each
+    // at 32 rows), so a job of few tiles finishes sooner with shorter ones; a
+    // job that fills the GPU gains nothing from them and pays their overhead.
+    // Measured: 256x256 frames 57 -> 41 us (8 rows), 512x512 71 -> 51 us (8 rows),
+    // 800x600 47 -> 40 us (16 rows), 1920x1080 best at 32 rows.
+    uint32_t th = S.tile_rows;
+    if (th == 0) {
+        const uint64_t slots = 4ull * (uint64_t)(c->nsm > 0 ? c->nsm : 1);
+        th = 8;
+        for (uint32_t cand : {32u, 16u}) {
+            uint64_t tiles = 0;
+            for (uint32_t i = 0; i < n; i++)
+                tiles += ((targets[i].w + DG_TILE_W - 1) / DG_TILE_W) * ((targets[i].h + cand - 1) / cand);
+            if (tiles >= slots) {
+                th = cand;
+                break;
+            }
+        }
+    }
     for (uint32_t i = 0; i < n; i++) {
         Scene& s = *scenes[i];  // frame_setup updates the camera basis, as Scene::render does
         const FrameTarget& tg = targets[i];
@@ -561,7 +582,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         f.seg_begin = (uint32_t)segs.size();
         f.tile_begin = (uint32_t)total_tiles;
         f.tiles_x = (uint32_t)((tg.w + DG_TILE_W - 1) / DG_TILE_W);
-        total_tiles += (uint64_t)f.tiles_x * ((tg.h + S.tile_rows - 1) / S.tile_rows);
+        total_tiles += (uint64_t)f.tiles_x * ((tg.h + th - 1) / th);
         f.pix_begin = (uint32_t)total_px;
         total_px += tg.w * tg.h;
         if (total_px >= 0x80000000ull) return DG_E_LIMIT;  // job-wide pixel indices use 31 bits
@@ -730,7 +751,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.item_units = S.item_units;
     job.cnt = S.d_counters;
     job.total_px = (uint32_t)total_px;
-    job.tile_rows = S.tile_rows;
+    job.tile_rows = th;
     job.tex = c->d_tex;
     job.ntex = (uint32_t)c->tex.size();
     job.err = S.d_err;
@@ -979,7 +1000,7 @@ dg_status dg_ctx_set_tuning(dg_ctx* c, const dg_tuning* t) {
     if (!c || !t) return DG_E_INVALID;
     auto bad = [](uint32_t b) { return b < 1 || b > 64; };
     if (t->small_max_px > 4096 || bad(t->setup_blocks_per_sm) || bad(t->queue_blocks_per_sm) ||
-        bad(t->cull_blocks_per_sm) || (t->tile_rows != 8 && t->tile_rows != 16 && t->tile_rows != 32) ||
+        bad(t->cull_blocks_per_sm) || (t->tile_rows != 0 && t->tile_rows != 8 && t->tile_rows != 16 && t->tile_rows != 32) ||
         t->item_units < 1 || t->item_units > 256)
         return DG_E_INVALID;
     c->main.small_max_px = t->small_max_px;

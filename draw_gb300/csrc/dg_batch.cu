@@ -310,7 +310,7 @@ dg_status dg_autotune(dg_ctx* c, const int32_t* scenes, const int32_t* canvases,
         {&dg_tuning::queue_blocks_per_sm, {2, 4, 8, 16}},
         {&dg_tuning::setup_blocks_per_sm, {1, 2, 4, 8}},
         {&dg_tuning::cull_blocks_per_sm, {4, 8, 16, 32}},
-        {&dg_tuning::tile_rows, {8, 16, 32}},
+        {&dg_tuning::tile_rows, {0, 8, 16, 32}},
     };
     float cur_ms = 0.0f;
     e = time_tuning(c, scenes, canvases, n, reps, e0, e1, &cur_ms);

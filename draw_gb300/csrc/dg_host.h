@@ -170,7 +170,7 @@ struct JobSlot {
     uint32_t setup_blocks_per_sm = DG_SETUP_BLOCKS_PER_SM;
     uint32_t queue_blocks_per_sm = DG_QUEUE_BLOCKS_PER_SM;
     uint32_t cull_blocks_per_sm = DG_CULL_BLOCKS_PER_SM;
-    uint32_t tile_rows = DG_TILE_H;
+    uint32_t tile_rows = 0;  // 0: chosen per job (build_job)
     uint32_t item_units = DG_ITEM_UNITS;
     uint32_t record_limit = 0;
     unsigned long long* d_counters = nullptr;  // DG_NCOUNTERS job counters (DG_CNT_*)

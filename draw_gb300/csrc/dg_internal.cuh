@@ -50,8 +50,9 @@ __device__ __forceinline__ bool dg_check_range(bool ok, uint32_t* err) {
 #define DG_SMALL_MAX_PX 16u
 #define DG_UNIT_PX 32u
 #define DG_ITEM_UNITS 8u
-// Resolve tile: 32 x tile_rows pixels (tile_rows 8, 16 or 32; default
-// DG_TILE_H), one CTA of 256 threads.
+// Resolve tile: 32 x tile_rows pixels (tile_rows 8, 16 or 32, chosen per job
+// unless the tuning fixes it; DG_TILE_H in the no-allocation path), one CTA of
+// 256 threads.
 #define DG_TILE_W 32u
 #define DG_TILE_H 32u
 #define DG_PACK_SHIFT 40

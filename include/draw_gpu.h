@@ -97,7 +97,8 @@ dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
  * passes in 256-thread blocks per SM (1..64); record_limit: 0, or at most this
  * many triangle records per render (triangles beyond it are shaded from the
  * mesh again in the resolve pass); tile_rows: height of the resolve pass's
- * 32-pixel-wide tiles (8, 16 or 32); item_units: 32-pixel units per work item
+ * 32-pixel-wide tiles (8, 16 or 32; 0, the default: per render job, the tallest
+ * whose tiles fill 4 resolve blocks per SM, else 8); item_units: 32-pixel units per work item
  * of the queue pass (1..256). Results do not depend on them. */
 typedef struct {
     uint32_t small_max_px;

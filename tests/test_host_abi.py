@@ -155,12 +155,12 @@ def test_tuning_round_trip_and_validation(lib):
     h = host_ctx(lib)
     t = (ctypes.c_uint32 * 7)()
     assert lib.dg_ctx_get_tuning(h, t) == 0
-    assert list(t) == [16, 4, 8, 32, 0, 32, 8]
+    assert list(t) == [16, 4, 8, 32, 0, 0, 8]  # tile_rows 0: chosen per render job
     good = (0, 1, 64, 2, 7, 16, 256)
     assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*good)) == 0
     assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
     for bad in ((4097, 16, 8, 32, 0, 8, 8), (32, 0, 8, 32, 0, 8, 8), (32, 16, 65, 32, 0, 8, 8),
-                (32, 16, 8, 0, 0, 8, 8), (32, 16, 8, 8, 0, 0, 8), (32, 16, 8, 8, 0, 12, 8),
+                (32, 16, 8, 0, 0, 8, 8), (32, 16, 8, 8, 0, 4, 8), (32, 16, 8, 8, 0, 12, 8),
                 (32, 16, 8, 8, 0, 64, 8), (32, 16, 8, 8, 0, 8, 0), (32, 16, 8, 8, 0, 8, 257)):
         assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*bad)) == 1
     assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
