@@ -173,7 +173,7 @@ struct JobSlot {
     uint32_t tile_rows = 0;  // 0: chosen per job (build_job)
     uint32_t item_units = DG_ITEM_UNITS;
     uint32_t record_limit = 0;
-    unsigned long long* d_counters = nullptr;  // DG_NCOUNTERS job counters (DG_CNT_*)
+    unsigned long long* d_counters = nullptr;  // the job counters (DG_CNT_*, DG_NCOUNTERS words)
     uint32_t* d_err = nullptr;
     static const int kStage = 4;  // pinned staging ring for job descriptors
     void* h_stage[kStage] = {};

@@ -199,18 +199,22 @@ struct alignas(16) DgQueueRec {
 };
 
 #define DG_NONE 0xFFFFFFFFu
-// Job counters (unsigned long long each).
-#define DG_CNT_QUEUE 0    // (queued records << DG_PACK_SHIFT) | work items
-#define DG_CNT_COVERED 1  // covered pixels (shaded by the resolve pass)
-#define DG_CNT_INPLACE 2  // large triangles rasterized by their own lane (queue or record overflow)
-#define DG_CNT_SURV 3     // triangles that passed the cull pass
-#define DG_CNT_TREC 4     // triangle records requested (statistics)
-#define DG_CNT_VROW 5     // light/halfway rows handed out to clip vertices
-#define DG_CNT_UNITS 6    // work units of the queued triangles
-#define DG_CNT_SMALL 7    // entries of the small-triangle list
-#define DG_CNT_TRECX 8    // records handed out after the first total_tri (multi-output clips)
-#define DG_CNT_TFRAG 10   // transparent fragments emitted
-#define DG_NCOUNTERS 12
+// Job counters (unsigned long long each), each on its own 128-byte line: the
+// hot ones take one atomic per warp or block from every pass, and counters that
+// share a line share one L2 slice, which serializes their updates (measured: the
+// setup pass of the 3840x2160 frame of 10M micro triangles, 702 -> 639 us).
+#define DG_CNT_LINE 16
+#define DG_CNT_QUEUE (0 * DG_CNT_LINE)    // (queued records << DG_PACK_SHIFT) | work items
+#define DG_CNT_COVERED (1 * DG_CNT_LINE)  // covered pixels (shaded by the resolve pass)
+#define DG_CNT_INPLACE (2 * DG_CNT_LINE)  // large triangles rasterized by their own lane (queue or record overflow)
+#define DG_CNT_SURV (3 * DG_CNT_LINE)     // triangles that passed the cull pass
+#define DG_CNT_TREC (4 * DG_CNT_LINE)     // triangle records requested (statistics)
+#define DG_CNT_VROW (5 * DG_CNT_LINE)     // light/halfway rows handed out to clip vertices
+#define DG_CNT_UNITS (6 * DG_CNT_LINE)    // work units of the queued triangles
+#define DG_CNT_SMALL (7 * DG_CNT_LINE)    // entries of the small-triangle list
+#define DG_CNT_TRECX (8 * DG_CNT_LINE)    // records handed out after the first total_tri (multi-output clips)
+#define DG_CNT_TFRAG (10 * DG_CNT_LINE)   // transparent fragments emitted
+#define DG_NCOUNTERS (12 * DG_CNT_LINE)   // words of the counter array (k_vertex zeroes them: <= 256)
 
 struct DgJobDev {
     const DgFrameDev* frames;
@@ -244,7 +248,7 @@ struct DgJobDev {
     uint32_t item_units;    // work units per raster work item (>= 1)
     uint32_t total_px;      // pixels of all frames
     uint32_t tile_rows;     // resolve tile height (8, 16 or 32)
-    unsigned long long* cnt;  // DG_NCOUNTERS job counters, zero at the start of the job
+    unsigned long long* cnt;  // the job counters (DG_CNT_*, DG_NCOUNTERS words), zero at the start of the job
     const DgTexDev* tex;
     uint32_t ntex;          // entries of tex
     uint32_t* err;

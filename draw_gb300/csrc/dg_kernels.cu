@@ -71,6 +71,7 @@ __global__ void __launch_bounds__(256, 8) k_vertex(const __grid_constant__ DgJob
                                                    const __grid_constant__ DgInlineDesc in) {
     allow_next_kernel();
     if (blockIdx.x == 0) {
+        static_assert(DG_NCOUNTERS <= 256, "block 0 of k_vertex zeroes the counters");
         if (threadIdx.x < DG_NCOUNTERS) job.cnt[threadIdx.x] = 0ull;
         if (in.nsegs) {
             constexpr uint32_t fw = sizeof(DgFrameDev) / 8, sw = sizeof(DgSegDev) / 8;
