@@ -914,7 +914,6 @@ template <uint32_t TH, bool EXT, bool LAZY>
 __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
     __shared__ float inv255[256];
     __shared__ DgTexDev stex[DG_SMEM_TEX];
-    resolve_prologue(job, inv255, stex);
     if (job.ntt == 0u) {
         // A tile that no triangle box reached is cleared before waiting for the
         // raster pass: its keys are all empty, and the cell map it reads is complete
@@ -927,10 +926,11 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJo
         const uint32_t lt = tile - fr.tile_begin;
         const uint32_t ty = lt / fr.tiles_x, tx = lt - ty * fr.tiles_x;
         if (fr.cells != nullptr && __ldcg(fr.cells + ((ty * TH) >> 5) * fr.tiles_x + tx) != fr.epoch) {
-            clear_tile<TH>(fr, tx, ty);
+            clear_tile<TH>(fr, tx, ty);  // (block-uniform) without the shading tables
             return;
         }
     }
+    resolve_prologue(job, inv255, stex);
     wait_previous_kernel();
     dev_resolve_tile<TH, EXT, LAZY>(job, blockIdx.x, inv255, stex);
 }
