@@ -307,7 +307,7 @@ dg_status dg_autotune(dg_ctx* c, const int32_t* scenes, const int32_t* canvases,
     const Knob knobs[] = {
         {&dg_tuning::small_max_px, {0, 4, 16, 64, 256}},
         {&dg_tuning::item_units, {2, 4, 8, 16, 32}},
-        {&dg_tuning::queue_blocks_per_sm, {2, 4, 8, 16}},
+        {&dg_tuning::queue_blocks_per_sm, {4, 8, 12, 16}},
         {&dg_tuning::setup_blocks_per_sm, {1, 2, 4, 8}},
         {&dg_tuning::cull_blocks_per_sm, {4, 8, 16, 32}},
         {&dg_tuning::tile_rows, {0, 8, 16, 32}},

@@ -155,7 +155,7 @@ def test_tuning_round_trip_and_validation(lib):
     h = host_ctx(lib)
     t = (ctypes.c_uint32 * 7)()
     assert lib.dg_ctx_get_tuning(h, t) == 0
-    assert list(t) == [16, 4, 8, 32, 0, 0, 8]  # tile_rows 0: chosen per render job
+    assert list(t) == [16, 4, 12, 32, 0, 0, 8]  # tile_rows 0: chosen per render job
     good = (0, 1, 64, 2, 7, 16, 256)
     assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*good)) == 0
     assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
