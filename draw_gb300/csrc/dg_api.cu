@@ -569,6 +569,9 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
                 f.flags |= DG_FRAME_LAZY;
                 any_lazy = true;
             }
+            f.small_max_px = S.small_max_px != DG_SMALL_MAX_PX_AUTO ? S.small_max_px
+                             : frame_tris >= tg.w * tg.h             ? DG_SMALL_MAX_PX_MICRO
+                                                                     : DG_SMALL_MAX_PX;
         }
         f.off_x = tg.off_x;
         f.off_y = tg.off_y;
@@ -747,7 +750,6 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
     job.items = S.d_items;
     job.items_cap = (uint32_t)std::min<size_t>(S.items_cap, 0xFFFFFFF0ull);
     job.queue_cap = (uint32_t)std::min<size_t>(S.queue_cap, (1u << 24) - 1);
-    job.small_max_px = S.small_max_px;
     job.item_units = S.item_units;
     job.cnt = S.d_counters;
     job.total_px = (uint32_t)total_px;
@@ -999,7 +1001,8 @@ dg_status dg_ctx_kernel_times(dg_ctx* c, float* ms, int32_t n) {
 dg_status dg_ctx_set_tuning(dg_ctx* c, const dg_tuning* t) {
     if (!c || !t) return DG_E_INVALID;
     auto bad = [](uint32_t b) { return b < 1 || b > 64; };
-    if (t->small_max_px > 4096 || bad(t->setup_blocks_per_sm) || bad(t->queue_blocks_per_sm) ||
+    if ((t->small_max_px > 4096 && t->small_max_px != DG_SMALL_MAX_PX_AUTO) || bad(t->setup_blocks_per_sm) ||
+        bad(t->queue_blocks_per_sm) ||
         bad(t->cull_blocks_per_sm) || (t->tile_rows != 0 && t->tile_rows != 8 && t->tile_rows != 16 && t->tile_rows != 32) ||
         t->item_units < 1 || t->item_units > 256)
         return DG_E_INVALID;

@@ -166,7 +166,7 @@ struct JobSlot {
     size_t trec_w_cap = 0;
     float4* d_ttrec_w = nullptr;  // the same for the transparent records
     size_t ttrec_w_cap = 0;
-    uint32_t small_max_px = DG_SMALL_MAX_PX;  // dg_tuning knobs
+    uint32_t small_max_px = DG_SMALL_MAX_PX_AUTO;  // dg_tuning knobs
     uint32_t setup_blocks_per_sm = DG_SETUP_BLOCKS_PER_SM;
     uint32_t queue_blocks_per_sm = DG_QUEUE_BLOCKS_PER_SM;
     uint32_t cull_blocks_per_sm = DG_CULL_BLOCKS_PER_SM;

@@ -41,13 +41,20 @@ __device__ __forceinline__ bool dg_check_range(bool ok, uint32_t* err) {
 }
 #define DG_VIS_EMPTY 0xFFFFFFFFFFFFFFFFull
 
-// Triangles whose clipped bounding box has at most this many pixels go to the
-// small-triangle list, whose entries the queue pass rasterizes one per lane
-// (default of DgJobDev.small_max_px); larger ones go to the raster queue: their
-// row-major bounding-box pixels are cut into units of DG_UNIT_PX (one per lane
-// of a warp) and the units into work items of at most DgJobDev.item_units
-// (default DG_ITEM_UNITS), which the queue pass spreads over all warps.
+// Triangles whose clipped bounding box has at most DgFrameDev.small_max_px
+// pixels go to the small-triangle list, whose entries the queue pass
+// rasterizes one per lane; larger ones go to the raster queue: their row-major
+// bounding-box pixels are cut into units of DG_UNIT_PX (one per lane of a warp)
+// and the units into work items of at most DgJobDev.item_units (default
+// DG_ITEM_UNITS), which the queue pass spreads over all warps. Unless the
+// tuning fixes it, a frame's threshold is DG_SMALL_MAX_PX, or
+// DG_SMALL_MAX_PX_MICRO when the frame has at least as many triangles as
+// pixels: lanes that each loop over a box of up to 64 pixels pay off only when
+// there are millions of such boxes to sort by size (the 3840x2160 frame of 10M
+// micro triangles 1,533 -> 1,423 us), while a frame of few small triangles
+// waits on its longest lane (the headline frame 88 -> 107 us at 64).
 #define DG_SMALL_MAX_PX 16u
+#define DG_SMALL_MAX_PX_MICRO 64u
 #define DG_UNIT_PX 32u
 #define DG_ITEM_UNITS 8u
 // Resolve tile: 32 x tile_rows pixels (tile_rows 8, 16 or 32, chosen per job
@@ -101,7 +108,7 @@ struct alignas(16) DgFrameDev {
     // its keys. Null: every tile takes the full path.
     uint32_t* cells;
     uint32_t flags;  // DG_FRAME_PERSPECTIVE: perspective-correct shading attributes (extension)
-    uint32_t pad;
+    uint32_t small_max_px;  // this frame's small-triangle threshold (bounding-box pixels, <= 4096)
 };
 #define DG_FRAME_PERSPECTIVE 1u
 // The frame has at least as many triangles as pixels: its small triangles
@@ -244,7 +251,6 @@ struct DgJobDev {
     uint32_t items_cap;
     DgQueueRec* small;      // small-triangle list (nunits unused), rasterized one triangle per lane
     uint32_t small_cap;
-    uint32_t small_max_px;  // small-triangle threshold (bounding-box pixels)
     uint32_t item_units;    // work units per raster work item (>= 1)
     uint32_t total_px;      // pixels of all frames
     uint32_t tile_rows;     // resolve tile height (8, 16 or 32)

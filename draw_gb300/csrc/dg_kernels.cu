@@ -316,7 +316,7 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
                         make_edges(tr.ax, tr.ay, tr.bx, tr.by, tr.cx, tr.cy, e);
                         const uint64_t px = (uint64_t)(tr.xhi - tr.xlo + 1u) * (uint64_t)(tr.yhi - tr.ylo + 1u);
                         if ((fr.flags & DG_FRAME_LAZY) && !clipped) {
-                            if (rbase != DG_NONE && px <= job.small_max_px) {
+                            if (rbase != DG_NONE && px <= fr.small_max_px) {
                                 e.tie |= DG_TRI_LAZY;  // no rows: shading computes the vertices' vectors
                             } else {
                                 const uint32_t vv[3] = {sg.vtx_begin + tp.x, sg.vtx_begin + tp.y, sg.vtx_begin + tp.z};
@@ -335,7 +335,7 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
                         }
                         if (rbase == DG_NONE) {
                             inplace = true;
-                        } else if (px <= job.small_max_px) {
+                        } else if (px <= fr.small_max_px) {
                             small = true;
                         } else {
                             qpx = (uint32_t)px;  // below 2^31: the canvas has fewer pixels

@@ -168,6 +168,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     f.tile_begin = 0;
     f.tiles_x = (p->canvas_width + DG_TILE_W - 1) / DG_TILE_W;
     f.pix_begin = 0;
+    f.small_max_px = DG_SMALL_MAX_PX;
     const uint32_t tiles = f.tiles_x * ((p->canvas_height + DG_TILE_H - 1) / DG_TILE_H);
 
     DgSegDev& sg = d.seg;
@@ -238,7 +239,6 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     job.items = reinterpret_cast<uint2*>(base + kOffQbase);
     job.items_cap = (uint32_t)dg_items_cap(kQueueCap);
     job.queue_cap = kQueueCap;
-    job.small_max_px = DG_SMALL_MAX_PX;
     job.item_units = DG_ITEM_UNITS;
     job.cnt = reinterpret_cast<unsigned long long*>(base + kOffCounters);
     job.total_px = (uint32_t)npx;

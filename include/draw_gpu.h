@@ -92,7 +92,9 @@ dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
 /* Launch-shape knobs of the raster passes (chosen by dg_autotune below):
  * small_max_px: triangles whose clipped bounding box has at most this many
  * pixels are rasterized one triangle per lane, the others are cut into 32-pixel
- * units spread over all warps (0 = all cut into units, max 4096); setup_blocks_per_sm,
+ * units spread over all warps (0 = all cut into units, max 4096;
+ * DG_SMALL_MAX_PX_AUTO, the default: per frame, 64 when the frame has at least
+ * as many triangles as pixels, else 16); setup_blocks_per_sm,
  * queue_blocks_per_sm and cull_blocks_per_sm: grid sizes (caps) of those
  * passes in 256-thread blocks per SM (1..64); record_limit: 0, or at most this
  * many triangle records per render (triangles beyond it are shaded from the
@@ -100,6 +102,7 @@ dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
  * 32-pixel-wide tiles (8, 16 or 32; 0, the default: per render job, the tallest
  * whose tiles fill 4 resolve blocks per SM, else 8); item_units: 32-pixel units per work item
  * of the queue pass (1..256). Results do not depend on them. */
+#define DG_SMALL_MAX_PX_AUTO 0xFFFFFFFFu
 typedef struct {
     uint32_t small_max_px;
     uint32_t setup_blocks_per_sm;

@@ -155,7 +155,8 @@ def test_tuning_round_trip_and_validation(lib):
     h = host_ctx(lib)
     t = (ctypes.c_uint32 * 7)()
     assert lib.dg_ctx_get_tuning(h, t) == 0
-    assert list(t) == [16, 4, 12, 32, 0, 0, 8]  # tile_rows 0: chosen per render job
+    # small_max_px DG_SMALL_MAX_PX_AUTO and tile_rows 0: chosen per frame and per render job
+    assert list(t) == [0xFFFFFFFF, 4, 12, 32, 0, 0, 8]
     good = (0, 1, 64, 2, 7, 16, 256)
     assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*good)) == 0
     assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
@@ -164,5 +165,8 @@ def test_tuning_round_trip_and_validation(lib):
                 (32, 16, 8, 8, 0, 64, 8), (32, 16, 8, 8, 0, 8, 0), (32, 16, 8, 8, 0, 8, 257)):
         assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*bad)) == 1
     assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(good)
+    auto = (0xFFFFFFFF, 4, 12, 32, 0, 0, 8)
+    assert lib.dg_ctx_set_tuning(h, (ctypes.c_uint32 * 7)(*auto)) == 0
+    assert lib.dg_ctx_get_tuning(h, t) == 0 and list(t) == list(auto)
     assert lib.dg_ctx_set_tuning(h, None) == 1
     lib.dg_ctx_destroy(h)
