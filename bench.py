@@ -565,7 +565,7 @@ def batched_leg(ctx, stream, n_frames: int) -> dict:
            "graph_frames_per_s": n_frames / (graph_default_ms * 1e-3),
            "graph_tuned_frames_per_s": n_frames / (graph_tuned_ms * 1e-3),
            "graph_speedup": plain_ms / graph_ms_best, "graph_kernels_per_replay": int(ginfo["kernels_per_replay"]),
-           "autotuned": tuned, "autotune_s": tune_s,
+           "autotuned": tuning_view(tuned), "autotune_s": tune_s,
            "workload": "256 frames, side log-uniform 128..512, 1k..200k triangles (torus/sphere), "
                        "textures 256^2..1024^2 from a pool of 32; L2 not flushed (working set > L2); "
                        "batched = one launch per stage for all frames; graph = the same job replayed from a "
@@ -618,7 +618,7 @@ def stress_leg(ctx, stream, flush, peak: float, steps: int = 20, cpu: bool = Tru
                        "4 point lights; L2 flushed before every frame",
            "near_crossing": desc.near_crossing, "depth_complexity_est": desc.depth_complexity_est,
            "mean_tri_px_est": desc.mean_tri_px_est, "build_s": gen_s,
-           "ms_per_frame_default": ms_default, "ms_per_frame_tuned": ms_tuned, "autotuned": tuned,
+           "ms_per_frame_default": ms_default, "ms_per_frame_tuned": ms_tuned, "autotuned": tuning_view(tuned),
            "frames_per_s": 1000.0 / ms, "mtris_per_s": desc.n_tris / (ms * 1e-3) / 1e6,
            "mshaded_frags_per_s": stats["covered_pixels"] / (ms * 1e-3) / 1e6,
            "frame_roofline": {"achieved": ab["frame"] / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -856,6 +856,17 @@ def serving_leg(local: int, seconds: float = 4.0, rate: float = 2000.0, n_meshes
 
 
 _TRAFFIC = None
+
+
+def tuning_view(t: dict) -> dict:
+    """Tuning knobs for the JSON line: the per-frame small-triangle threshold
+    (DG_SMALL_MAX_PX_AUTO) and the per-job tile height (0) read "auto"."""
+    out = dict(t)
+    if out.get("small_max_px") == 0xFFFFFFFF:
+        out["small_max_px"] = "auto"
+    if out.get("tile_rows") == 0:
+        out["tile_rows"] = "auto"
+    return out
 
 
 def read_traffic(kernel: str):
