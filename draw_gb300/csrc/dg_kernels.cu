@@ -377,7 +377,7 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
                             for (uint32_t cx = lane; cx < lx; cx += 32u) lc[l0 + cy * lw + cx] = le;
                     }
                 }
-                // Queue this round's large triangles with one 64-bit atomic per warp: it hands out
+                // Queue the large triangles of this output index with one 64-bit atomic per warp: it hands out
                 // the queue records and their work items together; the warp then writes all its
                 // items, each lane taking every 32nd.
                 const unsigned qmask = __ballot_sync(FULL, nu != 0u);
