@@ -861,6 +861,8 @@ dg_status launch_frames(dg_ctx* c, JobSlot& S, Scene* const* scenes, const Frame
     S.last_tri = B.total_tri;
     S.last_h2d = need;
     S.last_launches = B.launches;
+    S.last_tile_rows = B.job.tile_rows;
+    S.last_small_max_px = B.frames.empty() ? 0 : B.frames[0].small_max_px;
     e = enqueue_job(B, S, S.d_stage[k], S.stream, S.timing);
     if (e) return e;
     advance_transparent(c, B);
@@ -1035,7 +1037,7 @@ dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
     DG_CUDA(cudaStreamSynchronize(S.stream));
     unsigned long long h[DG_NCOUNTERS];
     DG_CUDA(cudaMemcpy(h, S.d_counters, sizeof(h), cudaMemcpyDeviceToHost));
-    const uint64_t v[12] = {S.last_vtx,
+    const uint64_t v[14] = {S.last_vtx,
                             S.last_tri,
                             h[DG_CNT_QUEUE] >> DG_PACK_SHIFT,
                             h[DG_CNT_UNITS],
@@ -1046,8 +1048,10 @@ dg_status dg_ctx_last_stats(dg_ctx* c, uint64_t* out, int32_t n) {
                             h[DG_CNT_SURV],
                             h[DG_CNT_TREC],
                             h[DG_CNT_VROW],
-                            h[DG_CNT_SMALL]};
-    for (int i = 0; i < n && i < 12; i++) out[i] = v[i];
+                            h[DG_CNT_SMALL],
+                            S.last_tile_rows,
+                            S.last_small_max_px};
+    for (int i = 0; i < n && i < 14; i++) out[i] = v[i];
     return DG_OK;
 }
 

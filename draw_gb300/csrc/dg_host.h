@@ -185,6 +185,7 @@ struct JobSlot {
     cudaEvent_t ev[DG_NKERNELS + 1] = {};
     bool ev_valid = false;
     uint64_t last_vtx = 0, last_tri = 0, last_h2d = 0, last_launches = 0;
+    uint64_t last_tile_rows = 0, last_small_max_px = 0;  // the last job's resolve tile height, first frame's threshold
     uint64_t scratch_bytes = 0;  // device bytes held by the scratch buffers
 };
 

@@ -179,7 +179,8 @@ TUNING_KEYS = ["small_max_px", "setup_blocks_per_sm", "queue_blocks_per_sm", "cu
                "tile_rows", "item_units"]
 # dg_ctx_last_stats entries in order.
 STATS_KEYS = ["vertices", "triangles", "queued_triangles", "queued_units", "covered_pixels", "inplace_triangles",
-              "h2d_bytes", "launches", "survivors", "triangle_records", "clip_rows", "small_triangles"]
+              "h2d_bytes", "launches", "survivors", "triangle_records", "clip_rows", "small_triangles", "tile_rows",
+              "small_max_px"]
 
 
 def _chk(st: int, what: str):

@@ -115,13 +115,14 @@ typedef struct {
 dg_status dg_ctx_set_tuning(dg_ctx* ctx, const dg_tuning* t);
 dg_status dg_ctx_get_tuning(dg_ctx* ctx, dg_tuning* t);
 
-/* Counters of the last render (up to 12): [0] vertices, [1] input triangles, [2] triangles
+/* Counters of the last render (up to 14): [0] vertices, [1] input triangles, [2] triangles
  * queued for the load-balanced raster pass, [3] their 32-pixel work units, [4] covered
  * pixels (written by resolve), [5] triangles rasterized in place because the queue, the
  * small-triangle list or the triangle records were full, [6] host-to-device bytes of the
  * job descriptor, [7] kernels launched, [8] triangles that passed the cull pass,
  * [9] triangles (clip outputs counted one by one) that asked for a triangle record, [10] light/halfway rows handed out to clip vertices,
- * [11] triangles on the small-triangle list. Synchronizes. */
+ * [11] triangles on the small-triangle list, [12] the resolve tile height the job used,
+ * [13] the small-triangle threshold of its first frame. Synchronizes. */
 dg_status dg_ctx_last_stats(dg_ctx* ctx, uint64_t* out, int32_t n);
 
 /* Self-check of the division the raster pass uses for the barycentrics of a
