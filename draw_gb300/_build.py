@@ -5,7 +5,9 @@ library statically, e.g. a Rust crate's build.rs). build(checked=True) makes
 draw_gb300/_lib/libdrawgpu_checked.so instead: compiled with DRAW_CHECKED, its
 kernels test the indices of their gathers and scatters against the buffers'
 sizes and record DG_E_CUDA in the error word, skipping the access, where one is
-out of range.
+out of range. build(timeline=True) makes draw_gb300/_lib/libdrawgpu_timeline.so:
+compiled with DRAW_TIMELINE, its kernels record their block start, wait and end
+times for dg_timeline_read (python -m draw_gb300.timeline prints them).
 
 Floating-point flags are part of the contract with the reference's Rust
 semantics: -fmad=false (no FMA contraction on the device), IEEE division and
@@ -27,6 +29,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdrawgpu.so")
 ARCHIVE = os.path.join(LIBDIR, "libdrawgpu.a")
 CHECKED_LIB = os.path.join(LIBDIR, "libdrawgpu_checked.so")
+TIMELINE_LIB = os.path.join(LIBDIR, "libdrawgpu_timeline.so")
 SOURCES = ["dg_kernels.cu", "dg_api.cu", "dg_server.cu", "dg_noalloc.cu", "dg_batch.cu", "dg_transparent.cu",
            "dg_selfcheck.cu", "dg_loader.cpp"]
 HEADERS = ["dg_internal.cuh", "dg_host.h", "dg_device.cuh"]
@@ -54,13 +57,14 @@ def _stale(lib: str = LIB) -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force: bool = False, verbose: bool = False, extra: list | None = None, checked: bool = False) -> str:
-    lib = CHECKED_LIB if checked else LIB
+def build(force: bool = False, verbose: bool = False, extra: list | None = None, checked: bool = False,
+          timeline: bool = False) -> str:
+    lib = CHECKED_LIB if checked else TIMELINE_LIB if timeline else LIB
     if not force and not _stale(lib):
         return lib
     os.makedirs(LIBDIR, exist_ok=True)
-    tag = f"{os.getpid()}{'c' if checked else ''}"
-    extra = list(extra or []) + (["-DDRAW_CHECKED"] if checked else [])
+    tag = f"{os.getpid()}{'c' if checked else ''}{'t' if timeline else ''}"
+    extra = list(extra or []) + (["-DDRAW_CHECKED"] if checked else []) + (["-DDRAW_TIMELINE"] if timeline else [])
     objs = []
     cmds = []
     for s in SOURCES:
@@ -80,7 +84,7 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None,
     if r.returncode:
         sys.stderr.write(" ".join(link) + "\n" + r.stdout + r.stderr)
         raise RuntimeError("nvcc link failed")
-    if not checked:
+    if lib == LIB:
         atmp = ARCHIVE + f".{tag}.tmp.a"
         r = subprocess.run(["ar", "rcs", atmp, *objs], capture_output=True, text=True)
         if r.returncode:
@@ -98,4 +102,5 @@ def build(force: bool = False, verbose: bool = False, extra: list | None = None,
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
-                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None, checked="--checked" in sys.argv))
+                extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None, checked="--checked" in sys.argv,
+                timeline="--timeline" in sys.argv))

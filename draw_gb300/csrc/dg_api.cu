@@ -990,6 +990,21 @@ dg_status dg_ctx_set_timing(dg_ctx* c, int32_t enable) {
     return DG_OK;
 }
 
+dg_status dg_timeline_read(dg_ctx* c, uint64_t* out, int32_t n) {
+    if (!c || !out || n < 0) return DG_E_INVALID;
+    dg_status e = set_device(c);
+    if (e) return e;
+    unsigned long long h[DG_NKERNELS * 4];
+    cudaError_t ce = cudaSuccess;
+    if (!dg_timeline_copy(h, c->main.stream, &ce)) return DG_E_INVALID;  // not a DRAW_TIMELINE build
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return DG_E_CUDA;
+    }
+    for (int i = 0; i < n && i < DG_NKERNELS * 4; i++) out[i] = h[i] == ~0ull ? 0u : h[i];
+    return DG_OK;
+}
+
 dg_status dg_ctx_kernel_times(dg_ctx* c, float* ms, int32_t n) {
     if (!c || !ms || n < 0) return DG_E_INVALID;
     if (c->device < 0) return DG_E_CUDA;

@@ -39,6 +39,17 @@ __device__ __forceinline__ bool dg_check_range(bool ok, uint32_t* err) {
     if (!ok) atomicOr(err, 1u << 6 /* DG_E_CUDA */);
     return ok;
 }
+// DRAW_TIMELINE builds (draw_gb300/_build.py build(timeline=True)): each
+// kernel of a render job records in the global timer (ns) when its first block
+// started, when its first and its last block passed the wait for the previous
+// kernel, and when its last block finished (thread 0 of each block, with
+// atomics; they add a few microseconds to a frame). dg_timeline_read returns
+// the record. Off in the normal build.
+#ifdef DRAW_TIMELINE
+#define DG_TIMELINE 1
+#else
+#define DG_TIMELINE 0
+#endif
 #define DG_VIS_EMPTY 0xFFFFFFFFFFFFFFFFull
 
 // Triangles whose clipped bounding box has at most DgFrameDev.small_max_px
@@ -319,6 +330,10 @@ struct DgLaunchCfg {
 // first kernel zeroes the job counters when the job has vertices; the caller
 // zeroes them otherwise.
 cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev);
+// DRAW_TIMELINE builds: copies the kernel timeline (4 words per kernel, as
+// dg_timeline_read returns them) to out after s drains and clears it; false in
+// other builds.
+bool dg_timeline_copy(unsigned long long* out, cudaStream_t s, cudaError_t* err);
 // The transparent pass (dg_transparent.cu), in three parts launched by
 // dg_launch_job: part 0 after the opaque setup (painter's sort, gather,
 // transparent setup), part 1 after the opaque raster (fragment emission and

@@ -43,6 +43,40 @@ namespace {
 // with programmatic dependent launch.
 // seg(i) and frame(i) give the job's descriptors (from global memory, or from
 // k_vertex's parameter for a small job).
+#if DG_TIMELINE
+// [kernel][first start, first wait passed, last wait passed, last end]
+__device__ unsigned long long g_timeline[DG_NKERNELS][4] = {
+    {~0ull, ~0ull, 0ull, 0ull}, {~0ull, ~0ull, 0ull, 0ull}, {~0ull, ~0ull, 0ull, 0ull},
+    {~0ull, ~0ull, 0ull, 0ull}, {~0ull, ~0ull, 0ull, 0ull}};
+__device__ __forceinline__ unsigned long long timeline_now() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// A block's start on construction, its end on destruction (every return path).
+struct TimelineBlock {
+    int k;
+    __device__ explicit TimelineBlock(int kernel) : k(kernel) {
+        if (threadIdx.x == 0) atomicMin(&g_timeline[k][0], timeline_now());
+    }
+    __device__ ~TimelineBlock() {
+        if (threadIdx.x == 0) atomicMax(&g_timeline[k][3], timeline_now());
+    }
+};
+__device__ __forceinline__ void timeline_waited(int k) {
+    if (threadIdx.x == 0) {
+        const unsigned long long t = timeline_now();
+        atomicMin(&g_timeline[k][1], t);
+        atomicMax(&g_timeline[k][2], t);
+    }
+}
+#define DG_TL_BLOCK(k) TimelineBlock dg_timeline_block_(k)
+#define DG_TL_WAITED(k) timeline_waited(k)
+#else
+#define DG_TL_BLOCK(k) ((void)0)
+#define DG_TL_WAITED(k) ((void)0)
+#endif
+
 template <class SEG, class FRM>
 __device__ __forceinline__ void dev_vertex(const DgJobDev& job, uint32_t nsegs, SEG seg, FRM frame) {
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -69,7 +103,9 @@ __device__ __forceinline__ void dev_vertex(const DgJobDev& job, uint32_t nsegs, 
 // `in` to job.frames and job.segs.
 __global__ void __launch_bounds__(256, 8) k_vertex(const __grid_constant__ DgJobDev job,
                                                    const __grid_constant__ DgInlineDesc in) {
+    DG_TL_BLOCK(0);
     allow_next_kernel();
+    DG_TL_WAITED(0);  // the first kernel of a job waits on nothing (a stream-ordered launch)
     if (blockIdx.x == 0) {
         static_assert(DG_NCOUNTERS <= 256, "block 0 of k_vertex zeroes the counters");
         if (threadIdx.x < DG_NCOUNTERS) job.cnt[threadIdx.x] = 0ull;
@@ -153,7 +189,9 @@ __device__ __forceinline__ void dev_cull(const DgJobDev& job) {
 }
 
 __global__ void __launch_bounds__(256) k_cull(const DgJobDev job) {
+    DG_TL_BLOCK(1);
     wait_previous_kernel();
+    DG_TL_WAITED(1);
     dev_cull(job);
 }
 
@@ -490,7 +528,9 @@ __device__ __forceinline__ void dev_setup(const DgJobDev& job) {
 }
 
 __global__ void __launch_bounds__(256) k_setup_raster(const DgJobDev job) {
+    DG_TL_BLOCK(2);
     wait_previous_kernel();
+    DG_TL_WAITED(2);
     dev_setup(job);
 }
 
@@ -699,7 +739,9 @@ __device__ __forceinline__ void dev_queue(const DgJobDev& job) {
 // the setup pass, so that its early clear of untouched tiles (k_resolve) reads
 // a complete cell map: the wait comes before the launch signal here.
 __global__ void __launch_bounds__(256, 4) k_queue_raster(const DgJobDev job) {
+    DG_TL_BLOCK(3);
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    DG_TL_WAITED(3);
     allow_next_kernel();
     dev_queue(job);
 }
@@ -912,6 +954,7 @@ __device__ __forceinline__ void dev_resolve_tile(const DgJobDev& job, const uint
 
 template <uint32_t TH, bool EXT, bool LAZY>
 __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJobDev job) {
+    DG_TL_BLOCK(4);  // tiles cleared before the wait record no wait
     __shared__ float inv255[256];
     __shared__ DgTexDev stex[DG_SMEM_TEX];
     if (job.ntt == 0u) {
@@ -932,6 +975,7 @@ __global__ void __launch_bounds__(256, 4) k_resolve(const __grid_constant__ DgJo
     }
     resolve_prologue(job, inv255, stex);
     wait_previous_kernel();
+    DG_TL_WAITED(4);
     dev_resolve_tile<TH, EXT, LAZY>(job, blockIdx.x, inv255, stex);
 }
 
@@ -964,6 +1008,26 @@ struct NvtxRange {
     explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
     ~NvtxRange() { nvtxRangePop(); }
 };
+
+bool dg_timeline_copy(unsigned long long* out, cudaStream_t s, cudaError_t* err) {
+#if DG_TIMELINE
+    unsigned long long init[DG_NKERNELS][4];
+    for (int k = 0; k < DG_NKERNELS; k++) {
+        init[k][0] = init[k][1] = ~0ull;
+        init[k][2] = init[k][3] = 0ull;
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemcpyFromSymbol(out, g_timeline, sizeof(init));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_timeline, init, sizeof(init));
+    *err = e;
+    return true;
+#else
+    (void)out;
+    (void)s;
+    *err = cudaSuccess;
+    return false;
+#endif
+}
 
 cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStream_t s, cudaEvent_t* ev) {
     NvtxRange job_range("draw_gb300 render job");

@@ -37,6 +37,7 @@ SIGNATURES = {
     "dg_ctx_stream": (_P, [_P]),
     "dg_ctx_set_timing": (_i32, [_P, _i32]),
     "dg_ctx_kernel_times": (_i32, [_P, _P, _i32]),
+    "dg_timeline_read": (_i32, [_P, _P, _i32]),
     "dg_ctx_last_stats": (_i32, [_P, _P, _i32]),
     "dg_check_division": (_i32, [_P, _i32, _u64, _u64, _P, _P, _P]),
     "dg_ctx_set_tuning": (_i32, [_P, _P]),
@@ -225,6 +226,16 @@ class Context:
         ms = (ctypes.c_float * len(KERNELS))()
         _chk(self.lib.dg_ctx_kernel_times(self.h, ms, len(KERNELS)), "kernel_times")
         return dict(zip(KERNELS, list(ms)))
+
+    def timeline(self) -> dict:
+        """dg_timeline_read (DRAW_TIMELINE builds): per kernel, microseconds after the
+        first k_vertex block's start: (first block start, first wait passed, last
+        wait passed, last block end), None where nothing was recorded."""
+        raw = (ctypes.c_uint64 * (4 * len(KERNELS)))()
+        _chk(self.lib.dg_timeline_read(self.h, raw, len(raw)), "timeline")
+        t0 = raw[0]
+        return {k: tuple(None if raw[4 * i + j] == 0 or t0 == 0 else (raw[4 * i + j] - t0) / 1000.0
+                         for j in range(4)) for i, k in enumerate(KERNELS)}
 
     def set_tuning(self, **knobs):
         """Raster knobs (TUNING_KEYS): in-warp raster threshold (bounding-box pixels) and grid

@@ -89,6 +89,15 @@ void* dg_ctx_stream(dg_ctx* ctx);
  * events between kernels also stop their launch overlap, so frames are slower meanwhile. */
 dg_status dg_ctx_set_timing(dg_ctx* ctx, int32_t enable);
 dg_status dg_ctx_kernel_times(dg_ctx* ctx, float* ms, int32_t n);
+/* Kernel timeline of the render jobs since the last call, in builds made with
+ * DRAW_TIMELINE (draw_gb300/_build.py build(timeline=True)); other builds
+ * return DG_E_INVALID. out[4k .. 4k+3] for kernel k in the order of
+ * dg_ctx_kernel_times: the global timer (ns) when its first block started, when
+ * its first and its last block passed the wait for the previous kernel, and
+ * when its last block finished; 0 where nothing was recorded (a kernel that did
+ * not run; a resolve pass whose tiles were all cleared before the wait).
+ * Synchronizes the context's stream and clears the record. */
+dg_status dg_timeline_read(dg_ctx* ctx, uint64_t* out, int32_t n);
 /* Launch-shape knobs of the raster passes (chosen by dg_autotune below):
  * small_max_px: triangles whose clipped bounding box has at most this many
  * pixels are rasterized one triangle per lane, the others are cut into 32-pixel

@@ -143,6 +143,9 @@ def test_host_only_context_refuses_device_work(lib):
     n = ctypes.c_uint64()
     assert lib.dg_check_division(h, 1, 16, 1, ctypes.byref(n), None, None) == 6
     assert lib.dg_check_division(h, 4, 16, 1, ctypes.byref(n), None, None) == 1  # no such sample family
+    assert lib.dg_timeline_read(h, None, 4) == 1
+    tl = (ctypes.c_uint64 * 20)()
+    assert lib.dg_timeline_read(h, tl, 20) == 6  # no device here
     # a graph batch or an autotune run renders each canvas once: a repeated canvas is refused
     ids = (ctypes.c_int32 * 2)(0, 0)
     bp = ctypes.c_void_p()
