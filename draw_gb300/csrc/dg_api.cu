@@ -799,6 +799,7 @@ dg_status build_job(dg_ctx* c, JobSlot& S, Scene* const* scenes, const FrameTarg
         p.blocks = (unsigned)c->nsm * 8u;
         B.launches += 3 * (p.n_tsort + p.n_fsort) + 6;
     }
+    B.cfg.vertex_blocks = (unsigned)c->nsm * DG_VERTEX_BLOCKS_PER_SM;
     B.cfg.cull_blocks = (unsigned)c->nsm * S.cull_blocks_per_sm;
     B.cfg.setup_blocks = (unsigned)c->nsm * S.setup_blocks_per_sm;
     B.cfg.queue_blocks = (unsigned)c->nsm * S.queue_blocks_per_sm;

@@ -309,12 +309,17 @@ struct alignas(16) DgInlineDesc {
 
 // Host-side launchers (dg_kernels.cu).
 struct DgLaunchCfg {
-    unsigned cull_blocks;   // grid caps / sizes in 256-thread blocks
+    unsigned vertex_blocks;  // grid caps / sizes in 256-thread blocks
+    unsigned cull_blocks;
     unsigned setup_blocks;
     unsigned queue_blocks;
     const DgInlineDesc* inl;  // host memory, read at launch; null: descriptors already on the device
     DgTransparentPlan tplan;
 };
+// k_vertex's grid cap: its resident blocks (launch bounds 256 x 8), one wave
+// that loops over the vertices (measured against a block per 256 vertices: the
+// headline frame 88.8 -> 87.8 us, the stress frame's vertex pass 64 -> 59 us).
+#define DG_VERTEX_BLOCKS_PER_SM 8u
 #define DG_SETUP_BLOCKS_PER_SM 4u
 #define DG_CLIP_DEFER 512u  // k_setup_raster: clipped survivors a block sets up in its second pass
 // k_queue_raster's grid: 3 waves of its 4 resident blocks per SM. The passes'

@@ -1038,7 +1038,8 @@ cudaError_t dg_launch_job(const DgJobDev& job, const DgLaunchCfg& cfg, cudaStrea
         NvtxRange r("k_vertex");
         DgInlineDesc none;
         if (!cfg.inl) none.nsegs = 0;
-        k_vertex<<<grid_for(job.total_vtx, 1u << 20), 256, 0, s>>>(job, cfg.inl ? *cfg.inl : none);
+        const unsigned vb = cfg.vertex_blocks < 1u ? 1u : cfg.vertex_blocks;
+        k_vertex<<<grid_for(job.total_vtx, vb), 256, 0, s>>>(job, cfg.inl ? *cfg.inl : none);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if ((e = mark(1)) != cudaSuccess) return e;

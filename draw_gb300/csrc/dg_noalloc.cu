@@ -256,6 +256,7 @@ extern "C" dg_status dg_render_noalloc(const dg_frame_params* p, const dg_device
     NA_CUDA(cudaGetLastError());
 
     DgLaunchCfg cfg{};
+    cfg.vertex_blocks = (unsigned)nsm * DG_VERTEX_BLOCKS_PER_SM;
     cfg.cull_blocks = (unsigned)nsm * DG_CULL_BLOCKS_PER_SM;
     cfg.setup_blocks = (unsigned)nsm * DG_SETUP_BLOCKS_PER_SM;
     cfg.queue_blocks = (unsigned)nsm * DG_QUEUE_BLOCKS_PER_SM;
