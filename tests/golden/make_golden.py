@@ -35,6 +35,15 @@ def golden_cases():
     off = S.torus_scene(width=200, height=140, nu=20, nv=10, tex=32, exponent=2)
     off.offset, off.canvas_wh, off.clear_depth = (60, 40), (80, 60), 100000.0
     out["offset_collapse"] = off
+    # the opt-in extensions (no counterpart in the reference): perspective-correct
+    # interpolation, bilinear fetch, both; and the transparent pass
+    for name, interp, filt in (("ext_perspective", 1, 0), ("ext_bilinear", 0, 1), ("ext_both", 1, 1)):
+        d = S.torus_scene(width=160, height=120, nu=24, nv=10, tex=64)
+        d.interpolation = interp
+        for t in d.textures:
+            t.filter = filt
+        out[name] = d
+    out["transparent"] = cases.transparent_scene()
     return out
 
 

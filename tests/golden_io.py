@@ -16,10 +16,12 @@ def save(path, desc, bgra, depth, status=0):
         "offset": np.array(desc.offset, np.int32),
         "canvas_wh": np.array(desc.canvas_size, np.int64), "n_tex": len(desc.textures),
         "n_obj": len(desc.objects), "bgra": bgra, "depth": depth, "status": status,
+        "interpolation": int(getattr(desc, "interpolation", 0)),
     }
     for i, t in enumerate(desc.textures):
         d[f"tex{i}_img"] = t.img
         d[f"tex{i}_shape"] = np.array([t.width, t.height, t.comps], np.int64)
+        d[f"tex{i}_filter"] = int(getattr(t, "filter", 0))
     for i, o in enumerate(desc.objects):
         d[f"obj{i}_v"] = o.vertices
         d[f"obj{i}_n"] = o.normals
@@ -38,7 +40,10 @@ def load(path):
     textures = []
     for i in range(int(z["n_tex"])):
         w, h, c = (int(x) for x in z[f"tex{i}_shape"])
-        textures.append(S.TextureDesc(z[f"tex{i}_img"], w, h, c))
+        t = S.TextureDesc(z[f"tex{i}_img"], w, h, c)
+        if f"tex{i}_filter" in z.files:  # the opt-in bilinear filter (older fixtures: nearest)
+            t.filter = int(z[f"tex{i}_filter"])
+        textures.append(t)
     objects = []
     for i in range(int(z["n_obj"])):
         meshes = [S.MeshDesc(z[f"obj{i}_mesh{j}_tris"], int(z[f"obj{i}_mesh{j}_tex"]))
@@ -52,4 +57,6 @@ def load(path):
                        fov_x=float(z["fov_x"]), lights=z["lights"], exponent=int(z["exponent"]),
                        clear_depth=float(z["clear_depth"]), offset=tuple(int(x) for x in z["offset"]),
                        canvas_wh=(cw, ch), textures=textures, objects=objects)
+    if "interpolation" in z.files:  # the opt-in perspective-correct mode (older fixtures: screen space)
+        desc.interpolation = int(z["interpolation"])
     return desc, z["bgra"], z["depth"], int(z["status"])
