@@ -319,20 +319,23 @@ def run_ours(args, world, rank, local):
     if rank == 0 or not os.path.exists(_build.LIB):
         _build.build()
     barrier(world)
-    torch.cuda.set_device(local)
+    # one replica per rank; with more ranks than GPUs the replicas share devices
+    # (they never wait on one another)
+    dev = local % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
     dev_uuid = None
     try:
-        u = str(torch.cuda.get_device_properties(local).uuid)
+        u = str(torch.cuda.get_device_properties(dev).uuid)
         dev_uuid = u if u.startswith("GPU-") else "GPU-" + u
     except Exception:
         pass
     stream = torch.cuda.Stream()
-    ctx = renderer.Context(local)
+    ctx = renderer.Context(dev)
     ctx.set_stream(stream.cuda_stream)
     desc = headline_scene()
     built = renderer.build_scene(desc, ctx)
     scene, canvas = built.scene, built.canvas
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
     peak, peak_kind = measured_peak()
 
     clocks = ClockSampler(dev_uuid)
@@ -442,7 +445,7 @@ def run_ours(args, world, rank, local):
         line["batched"] = batched_leg(ctx, stream, args.batch_frames)
 
     if rank == 0 and world == 1 and not args.no_serve:
-        line["served"] = serving_leg(local, seconds=args.serve_seconds, rate=args.serve_rate,
+        line["served"] = serving_leg(dev, seconds=args.serve_seconds, rate=args.serve_rate,
                                      max_batch=args.serve_batch, streams=args.serve_streams)
 
     if rank == 0 and world == 1 and not args.no_stress:
